@@ -1,0 +1,170 @@
+/*
+ * sphx — GB300-native SPH step (C-ABI).
+ *
+ * Drop-in replacement for the per-step hot path of lijenicol/SPH-Fluid-Simulator:
+ * SPHSystem::update (src/SPHSystem.cpp:110-117) -> updateParticles
+ * (src/sph.cpp:277-290) -> updateParticlesCPU / updateParticlesGPU
+ * (src/sph.cpp:195-275, src/kernels/sphGPU.cu:244-309).  State stays resident
+ * on one GPU between steps; every entry point returns an int status
+ * (SPHX_OK = 0, negative on error, message in sphx_last_error()) where the
+ * reference returns void and checks nothing.
+ *
+ * Arrays crossing this boundary are host arrays unless named "device".  Vec3
+ * arrays hold 3 floats per particle (x, y, z); per-particle outputs are in id
+ * order (row i = the particle passed in row i at create / set_state), unlike
+ * the reference, whose particle array is permuted by its sort every step
+ * (src/sph.cpp:227).
+ */
+#ifndef SPHX_H
+#define SPHX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPHX_OK 0
+#define SPHX_ERR_INVALID (-1)  /* bad argument */
+#define SPHX_ERR_CUDA (-2)     /* CUDA runtime / no usable GPU */
+#define SPHX_ERR_NOMEM (-3)    /* device or pinned allocation failed */
+#define SPHX_ERR_DOMAIN (-4)   /* non-finite position or |x/h| >= 2^30 */
+#define SPHX_ERR_OVERFLOW (-5) /* a cell holds more particles than the limit */
+#define SPHX_ERR_STATE (-6)    /* handle state invalid after an earlier error */
+
+/* Constructor arguments of SPHSettings (src/SPHSystem.h:15-17). */
+typedef struct sphx_settings {
+    float mass, rest_density, gas_const, viscosity, h, g, tension;
+} sphx_settings;
+
+/* The fields SPHSettings derives (src/SPHSystem.h:19-21, SPHSystem.cpp:8-26),
+ * bit-identical to the reference's. sphere_scale is column-major. */
+typedef struct sphx_derived {
+    float poly6, spiky_grad, spiky_lap, gas_constant, mass, h2, self_dens,
+        rest_density, viscosity, h, g, tension, mass_poly6_product;
+    float sphere_scale[16];
+} sphx_derived;
+
+/* Wall geometry.  The reference hard-codes x, z in [-8, 8], a floor at y = 0,
+ * no ceiling, damping 0.5 and offset 1e-4 (src/sph.cpp:139-176); reflection
+ * happens at bound +- h.  sphx_box_reference() fills exactly that. */
+typedef struct sphx_box {
+    float xmin, xmax, ymin, ymax, zmin, zmax;
+    float damping; /* velocity factor on reflection (reference 0.5) */
+    float offset;  /* position offset on reflection (reference 1e-4) */
+    int has_ceiling; /* 0 in the reference: ymax unused */
+} sphx_box;
+
+typedef struct sphx_options {
+    int reorder_interval;  /* permute particle data into cell order every R steps (>= 1) */
+    int use_graph;         /* replay each step as a captured CUDA graph */
+    int device;            /* CUDA device ordinal */
+    void *stream;          /* cudaStream_t to run on; NULL: the handle owns one */
+    float grid_ymax;       /* top of the cell grid without a ceiling; <= ymin: automatic */
+    int grid_dims[3];      /* cell-grid dimensions; 0: automatic (each >= 5) */
+    int grid_origin[3];    /* cell coordinates of grid slot 0 (used when grid_dims set) */
+    uint32_t max_cell_occupancy; /* particles per cell before a step fails (0: 1024) */
+} sphx_options;
+
+/* Dam-break lattice block: index i + nx*(j + ny*k), position
+ * origin + (i, j, k) * spacing + jitter, jitter uniform in [-amp, amp) per
+ * axis from a SplitMix64 stream (counter 3*index + axis) seeded by `seed`. */
+typedef struct sphx_lattice_desc {
+    uint32_t nx, ny, nz;
+    float origin[3];
+    float spacing;
+    float jitter;
+    uint64_t seed;
+} sphx_lattice_desc;
+
+typedef struct sphx_handle sphx_handle;
+
+/* Device-resident state of a handle (float4 rows: x, y, z, 0), in the
+ * handle's current storage order; id[k] is the id of storage row k. */
+typedef struct sphx_device_view {
+    const void *pos;   /* float4[n] */
+    const void *vel;   /* float4[n] */
+    const void *force; /* float4[n], force of the last step */
+    const void *rho_prs; /* float2[n]: density, pressure of the last step */
+    const uint32_t *id; /* uint32[n] */
+    size_t n;
+    void *stream;      /* cudaStream_t the handle runs on */
+} sphx_device_view;
+
+/* Per-phase device time accumulated while profiling is on (ms, CUDA events
+ * on the handle's stream). */
+typedef struct sphx_kernel_times {
+    double sort_ms;    /* keys + scan + scatter + cell sort + reorder */
+    double density_ms; /* k_density */
+    double force_ms;   /* k_force (force + integrate + walls) */
+    uint64_t steps;
+    uint64_t launches; /* kernels launched by those steps */
+} sphx_kernel_times;
+
+const char *sphx_version(void);
+/* Message of the last error on the calling thread ("" if none). */
+const char *sphx_last_error(void);
+
+/* Tester.cpp:90: SPHSettings(0.02, 1000, 1, 1.04, 0.15, -9.8, 0.2). */
+void sphx_settings_reference(sphx_settings *s);
+void sphx_box_reference(sphx_box *b);
+void sphx_options_default(sphx_options *o);
+
+/* SPHSettings::SPHSettings (src/SPHSystem.cpp:8-26). */
+int sphx_derive(const sphx_settings *s, sphx_derived *out);
+/* getHash (src/neighborTable.cpp:5-12): the 18-bit value; the reference
+ * stores its low 16 bits (Particle.h:9). */
+uint32_t sphx_hash(int32_t cx, int32_t cy, int32_t cz);
+/* getCell (src/neighborTable.cpp:14-17): ivec3(p / h), truncating. */
+void sphx_cell(float x, float y, float z, float h, int32_t out[3]);
+/* Bucket-collision flags of the 27 cells around a cell (host evaluation of
+ * the test the kernels use): bit 0 = two neighbour cells share a bucket;
+ * bit 1+f = a cell two away across face f (-x,+x,-y,+y,-z,+z, only faces in
+ * face_mask) may share a visited bucket. */
+uint32_t sphx_collision_flags(int32_t cx, int32_t cy, int32_t cz, uint32_t face_mask);
+
+/* Fills 3*nx*ny*nz floats. */
+int sphx_lattice(const sphx_lattice_desc *d, float *pos3);
+/* SPHSystem::initParticles (src/SPHSystem.cpp:76-108): srand(1024), spacing
+ * h + 0.01, one-sided jitter; fills 3*W^3 floats (index i + (j + W*k)*W). */
+int sphx_reference_scene(size_t cube_width, float h, float *pos3);
+
+/* A resident scene of n particles (n >= 1).  vel3 may be NULL (zero).
+ * box NULL: the reference box; opt NULL: sphx_options_default. */
+int sphx_create(const sphx_settings *s, const sphx_box *box, const sphx_options *opt, size_t n,
+                const float *pos3, const float *vel3, sphx_handle **out);
+int sphx_destroy(sphx_handle *h);
+size_t sphx_count(const sphx_handle *h);
+/* Replaces positions / velocities (host, id order, vel3 may be NULL) and
+ * clears an error state. */
+int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3);
+/* Enqueues nsteps steps of dt (asynchronous; errors raised by the kernels
+ * surface at the next sphx_synchronize or read). */
+int sphx_step(sphx_handle *h, float dt, int nsteps);
+int sphx_synchronize(sphx_handle *h);
+/* Host readout in id order; any pointer may be NULL.  force3 / rho / prs are
+ * the values of the last step (what it integrated with). */
+int sphx_read_state(sphx_handle *h, float *pos3, float *vel3, float *rho, float *prs,
+                    float *force3);
+/* translate(position) * scale(h/2) per particle, 16 floats column-major, id
+ * order (src/sph.cpp:178-179) — the instanced renderer's input. */
+int sphx_read_transforms(sphx_handle *h, float *mat16);
+/* Cell (3 ints) and stored uint16 hash of each particle's current position,
+ * id order; either pointer may be NULL. */
+int sphx_read_cells(sphx_handle *h, int32_t *cells3, uint16_t *hash16);
+/* For the current positions: per particle, the number of accepted neighbour
+ * visits of the reference walk (src/sph.cpp:40-66) and the wrapping sum of
+ * SplitMix64-finalised ids over them (a multiset fingerprint), id order. */
+int sphx_neighbor_digest(sphx_handle *h, uint32_t *count, uint64_t *digest);
+int sphx_device_state(sphx_handle *h, sphx_device_view *out);
+
+int sphx_set_profiling(sphx_handle *h, int enable);
+/* Synchronises, then returns the accumulated per-phase times and resets them. */
+int sphx_get_kernel_times(sphx_handle *h, sphx_kernel_times *out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHX_H */

@@ -1,0 +1,163 @@
+// Shared host/device definitions of the SPH step: the reference's integer
+// cell hash, the cell function, the settings-derived constants, and the
+// GF(2) test that decides when the fast cell walk is exact.
+//
+// Reference semantics being reproduced (lijenicol/SPH-Fluid-Simulator):
+//   * getCell = ivec3(p / h), truncation toward zero     neighborTable.cpp:14-17
+//   * getHash = ((uint)(x*73856093) ^ (uint)(y*19349663) ^ (uint)(z*83492791))
+//               % 262144, stored in a uint16_t            neighborTable.cpp:5-12,
+//                                                          Particle.h:9, sph.cpp:43
+//   * a particle's neighbour candidates are all members of the 27 buckets
+//     hash16(cell + o), o in {-1,0,1}^3, visited once per offset, accepted
+//     when |pj - pi|^2 < h^2 in float                     sph.cpp:40-66, 90-127
+#pragma once
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define SPHX_HD __host__ __device__ __forceinline__
+#else
+#define SPHX_HD inline
+#endif
+
+namespace sphx {
+
+constexpr uint32_t kTableSize = 262144u;  // neighborTable.h:9
+constexpr uint32_t kHashP1 = 73856093u;   // neighborTable.cpp:8-10
+constexpr uint32_t kHashP2 = 19349663u;
+constexpr uint32_t kHashP3 = 83492791u;
+
+// Flag bits of a particle's cell (see collision_flags).
+constexpr uint32_t kFlagDup = 1u;          // two of the 27 neighbour cells share a bucket
+constexpr uint32_t kFlagFaceShift = 1u;    // bits 1..6: face (-x,+x,-y,+y,-z,+z)
+constexpr uint32_t kFlagNearShift = 8u;    // bits 8..13: particle within slack of that face
+
+// The hash the reference stores per particle: the low 16 bits of the xor of
+// three wrapped 32-bit products (% 262144 then uint16 truncation keeps the
+// low 16 bits).
+SPHX_HD uint32_t hash18(int x, int y, int z) {
+    return (((uint32_t)x * kHashP1) ^ ((uint32_t)y * kHashP2) ^ ((uint32_t)z * kHashP3)) &
+           (kTableSize - 1u);
+}
+SPHX_HD uint32_t hash16(int x, int y, int z) { return hash18(x, y, z) & 0xFFFFu; }
+
+// ivec3(p / h): IEEE division, then truncation toward zero.
+SPHX_HD float cell_quotient(float x, float h) {
+#if defined(__CUDA_ARCH__)
+    return __fdiv_rn(x, h);
+#else
+    return x / h;
+#endif
+}
+SPHX_HD int trunc_to_int(float q) {
+#if defined(__CUDA_ARCH__)
+    return __float2int_rz(q);
+#else
+    return (int)q;
+#endif
+}
+
+// xor-basis insertion ("x = min(x, x ^ b)" over the basis in insertion order
+// keeps every element reduced at the leading bits of the earlier ones).
+SPHX_HD uint32_t reduce6(uint32_t x, const uint32_t *b, int nb) {
+    for (int k = 0; k < 6; ++k)
+        if (k < nb) {
+            const uint32_t y = x ^ b[k];
+            x = y < x ? y : x;
+        }
+    return x;
+}
+
+// Bucket-collision structure of the 27 cells around (cx, cy, cz).
+//
+// With A[k] = low16((cx+k)*P1), B[k], C[k] likewise, hash16(cell+o) =
+// A[ox] ^ B[oy] ^ C[oz].  Two distinct offsets share a bucket iff a non-zero
+// combination of a1 = A[-1]^A[0], a2 = A[0]^A[1], b1, b2, c1, c2 xors to zero,
+// i.e. iff those six 16-bit vectors are linearly dependent over GF(2); then
+// kFlagDup is set and the reference visits some bucket twice.
+//
+// A cell two steps away across the +x face, (cx+2, cy+dy, cz+dz), can share
+// a bucket with one of the 27 only if A[1]^A[2] lies in the span of the six
+// vectors (necessary, not sufficient); likewise for the other five faces.
+// The matching face bit is set conservatively; the walk then checks the
+// actual hashes of the nine cells of that face.
+SPHX_HD uint32_t collision_flags(int cx, int cy, int cz, uint32_t face_mask) {
+    uint32_t A[5], B[5], C[5];
+    for (int k = 0; k < 5; ++k) {
+        A[k] = ((uint32_t)(cx + k - 2) * kHashP1) & 0xFFFFu;
+        B[k] = ((uint32_t)(cy + k - 2) * kHashP2) & 0xFFFFu;
+        C[k] = ((uint32_t)(cz + k - 2) * kHashP3) & 0xFFFFu;
+    }
+    const uint32_t v[6] = {A[1] ^ A[2], A[2] ^ A[3], B[1] ^ B[2],
+                           B[2] ^ B[3], C[1] ^ C[2], C[2] ^ C[3]};
+    uint32_t basis[6];
+    int nb = 0;
+    uint32_t flags = 0;
+    for (int i = 0; i < 6; ++i) {
+        const uint32_t x = reduce6(v[i], basis, nb);
+        if (x == 0u) flags |= kFlagDup;
+        else basis[nb++] = x;
+    }
+    const uint32_t f[6] = {A[0] ^ A[1], A[3] ^ A[4], B[0] ^ B[1],
+                           B[3] ^ B[4], C[0] ^ C[1], C[3] ^ C[4]};
+    for (int i = 0; i < 6; ++i)
+        if ((face_mask >> i) & 1u)
+            if (reduce6(f[i], basis, nb) == 0u) flags |= 1u << (kFlagFaceShift + i);
+    return flags;
+}
+
+// Whether a particle at quotient q (= x / h) in cell c = trunc(q) could be
+// within h, allowing for float rounding, of a particle in cell c - 2 (bit 0)
+// or c + 2 (bit 1).  Cell m covers [m, m+1) for m > 0, (m-1, m] for m < 0 and
+// (-1, 1) for m = 0 (truncation toward zero).  A particle of cell c+2 has a
+// quotient above (c+2 > 0 ? c+2 : c+1), so it can only be within one cell
+// width of q when q > (c+2 > 0 ? c+1 : c); symmetrically for c-2.  eps is
+// about 16x the worst-case rounding slack of the division and r^2 test.
+SPHX_HD uint32_t near_faces_1d(float q, int c) {
+    const float aq = q < 0.f ? -q : q;
+    const float eps = (aq + 8.0f) * 9.5367431640625e-07f;  // 2^-20
+    const float up = (float)((c + 2 > 0) ? c + 1 : c);
+    const float lo = (float)((c - 2 >= 0) ? c : c - 1);
+    return (q < lo + eps ? 1u : 0u) | (q > up - eps ? 2u : 0u);
+}
+
+// Constants of SPHSettings (SPHSystem.h:19-21), in the reference's order.
+struct Derived {
+    float poly6, spikyGrad, spikyLap, gasConstant, mass, h2, selfDens,
+        restDensity, viscosity, h, g, tension, massPoly6Product;
+};
+
+// SPHSystem.cpp:8-26.  pow(h, n) of a float runs in double; each result is
+// rounded to float on assignment; PI is the float literal 3.14159265f.
+Derived derive_constants(float mass, float restDensity, float gasConst,
+                         float viscosity, float h, float g, float tension);
+
+// Uniform cell grid that particle keys are taken modulo.  Cell (cx, cy, cz)
+// maps to slot ((cz-oz) mod gz, (cy-oy) mod gy, (cx-ox) mod gx); cells that
+// share a slot are at least gx-1 (gy-1, gz-1) cells apart, so with every
+// dimension >= 5 no particle of an aliased cell can pass the r^2 < h^2 test:
+// aliasing costs time, never exactness.
+struct Grid {
+    int ox, oy, oz;
+    int gx, gy, gz;
+};
+
+SPHX_HD int wrap_mod(int a, int m) {
+    int r = a % m;
+    return r < 0 ? r + m : r;
+}
+
+// Everything one step's kernels read, passed by value.
+struct StepParams {
+    // physics (SPHSettings)
+    float h, h2, mp6, selfDens, gasConstant, restDensity, mass, viscosity;
+    float spikyGrad, spikyLap, g, halfH;
+    // walls (sph.cpp:153-176 generalised): reflect below ylo / above yhi ...
+    float ylo, yhi, xlo, xhi, zlo, zhi, damping, offset;
+    int hasCeiling;
+    float dt;
+    Grid grid;
+    uint32_t n;
+};
+
+}  // namespace sphx
