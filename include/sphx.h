@@ -86,7 +86,7 @@ typedef struct sphx_device_view {
     const void *pos;   /* float4[n] */
     const void *vel;   /* float4[n] */
     const void *force; /* float4[n], force of the last step */
-    const void *rho_prs; /* float2[n]: density, pressure of the last step */
+    const void *rho_prs; /* float4[n]: density, pressure, 1/density, 0 of the last step */
     const uint32_t *id; /* uint32[n] */
     size_t n;
     void *stream;      /* cudaStream_t the handle runs on */
@@ -158,6 +158,19 @@ int sphx_read_cells(sphx_handle *h, int32_t *cells3, uint16_t *hash16);
  * SplitMix64-finalised ids over them (a multiset fingerprint), id order. */
 int sphx_neighbor_digest(sphx_handle *h, uint32_t *count, uint64_t *digest);
 int sphx_device_state(sphx_handle *h, sphx_device_view *out);
+
+/* The reference's GPU seam, updateParticlesGPU(Particle*, glm::mat4*, size_t,
+ * const SPHSettings&, float) (src/kernels/sphGPU.h:8-11): one step over the
+ * caller's host array of n 60-byte Particle records (Particle.h:4-10) and,
+ * if transforms16 is not NULL, its n column-major mat4 transforms, both
+ * updated in place.  Records keep their order; `hash` holds hash16 of each
+ * record's pre-step cell; `acceleration` is left untouched.  Device state is
+ * cached across calls (re-created when n, settings or box change).  box NULL:
+ * the reference CPU path's walls (src/sph.cpp:139-176). */
+int sphx_update_particles(void *particles, float *transforms16, size_t n,
+                          const sphx_settings *s, const sphx_box *box, float dt);
+/* Frees the state cached by sphx_update_particles. */
+int sphx_update_particles_release(void);
 
 int sphx_set_profiling(sphx_handle *h, int enable);
 /* Synchronises, then returns the accumulated per-phase times and resets them. */

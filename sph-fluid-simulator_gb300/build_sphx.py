@@ -54,12 +54,26 @@ def _compile(src, extra=()):
     return obj, True
 
 
-def build(verbose=False, ptxas_info=False):
-    """Compiles every translation unit under csrc/ and links lib/libsphx.so."""
+def build(verbose=False, ptxas_info=False, defines=(), lib=None, build_dir=None):
+    """Compiles every translation unit under csrc/ and links lib/libsphx.so.
+
+    ``defines`` (e.g. ``["SPHX_FORCE_MIN_BLOCKS=2"]``) and ``lib`` /
+    ``build_dir`` build a variant elsewhere, for tuning sweeps."""
+    global BUILD
+    lib = lib or LIB
+    saved = BUILD
+    BUILD = build_dir or BUILD
+    try:
+        return _build(verbose, ptxas_info, ["-D" + d for d in defines], lib)
+    finally:
+        BUILD = saved
+
+
+def _build(verbose, ptxas_info, dflags, LIB):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
-    extra = ["-Xptxas", "-v"] if ptxas_info else []
+    extra = (["-Xptxas", "-v"] if ptxas_info else []) + dflags
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         results = list(ex.map(lambda s: _compile(s, extra), srcs))
     objs = [o for o, _ in results]

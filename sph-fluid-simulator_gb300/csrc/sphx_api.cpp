@@ -17,25 +17,11 @@
 #include <string>
 #include <vector>
 
-#include "sphx.h"
-#include "sphx_common.h"
-#include "sphx_kernels.h"
+#include "sphx_internal.h"
 
 namespace {
 
 thread_local std::string g_err;
-
-int fail(int code, const std::string &msg) {
-    g_err = msg;
-    return code;
-}
-
-#define SPHX_CUDA(call)                                                                  \
-    do {                                                                                 \
-        const cudaError_t e_ = (call);                                                   \
-        if (e_ != cudaSuccess)                                                           \
-            return fail(SPHX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    } while (0)
 
 uint64_t mix64(uint64_t z) {  // SplitMix64 output function of state z - gamma
     z += 0x9E3779B97F4A7C15ull;
@@ -46,16 +32,14 @@ uint64_t mix64(uint64_t z) {  // SplitMix64 output function of state z - gamma
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-struct GraphEntry {
-    bool reorder;
-    int pv, idc;
-    uint32_t dt_bits;
-    cudaGraphExec_t exec;
-};
-
 }  // namespace
 
 namespace sphx {
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
 
 Derived derive_constants(float mass, float restDensity, float gasConst, float viscosity, float h,
                          float g, float tension) {
@@ -79,35 +63,7 @@ Derived derive_constants(float mass, float restDensity, float gasConst, float vi
 
 }  // namespace sphx
 
-struct sphx_handle {
-    sphx_settings s;
-    sphx::Derived d;
-    sphx_box box;
-    sphx_options opt;
-    uint32_t n = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    sphx::Grid grid{};
-    char *arena = nullptr;
-    float4 *pos[2] = {nullptr, nullptr};
-    float4 *vel[2] = {nullptr, nullptr};
-    uint32_t *id[2] = {nullptr, nullptr};
-    float2 *rp = nullptr;
-    float4 *force = nullptr;
-    float *staging = nullptr;     // 6n floats
-    float *transforms = nullptr;  // 16n floats, allocated on first use
-    sphx::SortBuffers sb{};
-    uint32_t *h_status = nullptr;  // pinned
-    int pv = 0, idc = 0;
-    uint64_t step_count = 0;
-    int error = 0;
-    bool profiling = false;
-    std::vector<cudaEvent_t> events;  // 4 per profiled step
-    std::vector<uint32_t> launches_per_step;
-    size_t events_used = 0;
-    sphx_kernel_times acc{};
-    std::vector<GraphEntry> graphs;
-};
+using sphx::fail;
 
 namespace {
 
@@ -193,6 +149,8 @@ sphx::StepParams make_params(const sphx_handle *h, float dt) {
     P.spikyLap = d.spikyLap;
     P.g = d.g;
     P.halfH = d.h / 2.f;
+    P.forceKp = 0.5f * d.mass * d.spikyGrad;
+    P.forceKv = d.viscosity * d.mass * d.spikyLap;
     // sph.cpp:153-176: y < h, x < h - 8, x > -h + 8, z likewise.
     P.ylo = h->box.ymin + d.h;
     P.yhi = h->box.ymax - d.h;
@@ -217,8 +175,8 @@ int upload(sphx_handle *h, const float *pos3, const float *vel3) {
                                   h->stream));
     SPHX_CUDA(sphx::launch_upload(h->n, h->staging, vel3 ? h->staging + 3 * n : nullptr,
                                   h->pos[h->pv], h->vel[h->pv], h->id[h->idc], h->stream));
-    SPHX_CUDA(cudaMemsetAsync(h->sb.status, 0, 4, h->stream));
-    SPHX_CUDA(cudaMemsetAsync(h->rp, 0, 8 * n, h->stream));
+    SPHX_CUDA(cudaMemsetAsync(h->sb.status, 0, 8, h->stream));
+    SPHX_CUDA(cudaMemsetAsync(h->rp, 0, 16 * n, h->stream));
     SPHX_CUDA(cudaMemsetAsync(h->force, 0, 16 * n, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));
     h->error = 0;
@@ -254,7 +212,7 @@ cudaError_t enqueue_step(sphx_handle *h, const sphx::StepParams &P, bool reorder
     return cudaSuccess;
 }
 
-int read_status(sphx_handle *h) {
+int read_status_impl(sphx_handle *h) {
     SPHX_CUDA(cudaMemcpyAsync(h->h_status, h->sb.status, 4, cudaMemcpyDeviceToHost, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));
     const uint32_t st = *h->h_status;
@@ -279,7 +237,7 @@ void destroy_graphs(sphx_handle *h) {
 int run_graph_step(sphx_handle *h, const sphx::StepParams &P, bool reorder) {
     uint32_t dt_bits;
     std::memcpy(&dt_bits, &P.dt, 4);
-    GraphEntry *hit = nullptr;
+    sphx::GraphEntry *hit = nullptr;
     for (auto &g : h->graphs)
         if (g.reorder == reorder && g.pv == h->pv && g.idc == h->idc && g.dt_bits == dt_bits)
             hit = &g;
@@ -292,7 +250,7 @@ int run_graph_step(sphx_handle *h, const sphx::StepParams &P, bool reorder) {
         const cudaError_t e2 = cudaStreamEndCapture(h->stream, &graph);
         if (e != cudaSuccess) return fail(SPHX_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
         if (e2 != cudaSuccess) return fail(SPHX_ERR_CUDA, std::string("end capture: ") + cudaGetErrorString(e2));
-        GraphEntry g{reorder, h->pv, h->idc, dt_bits, nullptr};
+        sphx::GraphEntry g{reorder, h->pv, h->idc, dt_bits, nullptr};
         const cudaError_t e3 = cudaGraphInstantiate(&g.exec, graph, 0ULL);
         cudaGraphDestroy(graph);
         if (e3 != cudaSuccess) return fail(SPHX_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(e3));
@@ -305,6 +263,12 @@ int run_graph_step(sphx_handle *h, const sphx::StepParams &P, bool reorder) {
     if (!reorder) h->pv ^= 1;
     return SPHX_OK;
 }
+
+}  // namespace
+
+int sphx::read_status(sphx_handle *h) { return read_status_impl(h); }
+
+namespace {
 
 #define HANDLE_CHECK(h)                                                 \
     do {                                                                \
@@ -450,7 +414,7 @@ int sphx_create(const sphx_settings *s, const sphx_box *box, const sphx_options 
     const size_t ntiles = (slots + 1 + 4095) / 4096;
     const size_t sizes[] = {16 * n, 16 * n, 16 * n, 16 * n,  // pos[2], vel[2]
                             4 * n,  4 * n,                    // id[2]
-                            8 * n,  16 * n,                   // rp, force
+                            16 * n, 16 * n,                   // rp, force
                             4 * n,  4 * n,  4 * n,            // key, rank, order
                             4 * (slots + 1), 4 * (slots + 1), // count, start
                             4 * ntiles, 256,                  // tile_sum, status
@@ -474,7 +438,7 @@ int sphx_create(const sphx_settings *s, const sphx_box *box, const sphx_options 
     h->vel[1] = (float4 *)ptrs[3];
     h->id[0] = (uint32_t *)ptrs[4];
     h->id[1] = (uint32_t *)ptrs[5];
-    h->rp = (float2 *)ptrs[6];
+    h->rp = (float4 *)ptrs[6];
     h->force = (float4 *)ptrs[7];
     h->sb.key = (uint32_t *)ptrs[8];
     h->sb.rank = (uint32_t *)ptrs[9];
@@ -542,6 +506,12 @@ int sphx_step(sphx_handle *h, float dt, int nsteps) {
     HANDLE_CHECK(h);
     if (h->error) return fail(SPHX_ERR_STATE, "handle is in an error state; call sphx_set_state");
     if (nsteps < 0 || !std::isfinite(dt)) return fail(SPHX_ERR_INVALID, "bad dt or step count");
+    return sphx::run_steps(h, dt, nsteps);
+}
+
+}  // extern "C"
+
+int sphx::run_steps(sphx_handle *h, float dt, int nsteps) {
     const sphx::StepParams P = make_params(h, dt);
     for (int k = 0; k < nsteps; ++k) {
         const bool reorder = (h->step_count % (uint64_t)h->opt.reorder_interval) == 0;
@@ -575,11 +545,13 @@ int sphx_step(sphx_handle *h, float dt, int nsteps) {
     return SPHX_OK;
 }
 
+extern "C" {
+
 int sphx_synchronize(sphx_handle *h) {
     HANDLE_CHECK(h);
     SPHX_CUDA(cudaStreamSynchronize(h->stream));
     if (h->error) return fail(h->error, "handle is in an error state; call sphx_set_state");
-    return read_status(h);
+    return sphx::read_status(h);
 }
 
 int sphx_read_state(sphx_handle *h, float *pos3, float *vel3, float *rho, float *prs,
@@ -651,7 +623,7 @@ int sphx_neighbor_digest(sphx_handle *h, uint32_t *count, uint64_t *digest) {
     SPHX_CUDA(sphx::launch_sort(P, h->sb, h->pos[h->pv], h->stream));
     SPHX_CUDA(sphx::launch_digest(P, h->sb, h->pos[h->pv], h->id[h->idc], dcount, ddig, true,
                                   h->stream));
-    rc = read_status(h);
+    rc = sphx::read_status(h);
     if (rc) return rc;
     SPHX_CUDA(cudaMemcpyAsync(count, dcount, 4 * n, cudaMemcpyDeviceToHost, h->stream));
     SPHX_CUDA(cudaMemcpyAsync(digest, ddig, 8 * n, cudaMemcpyDeviceToHost, h->stream));

@@ -152,6 +152,8 @@ struct StepParams {
     // physics (SPHSettings)
     float h, h2, mp6, selfDens, gasConstant, restDensity, mass, viscosity;
     float spikyGrad, spikyLap, g, halfH;
+    float forceKp;  // mass * spikyGrad / 2
+    float forceKv;  // viscosity * mass * spikyLap
     // walls (sph.cpp:153-176 generalised): reflect below ylo / above yhi ...
     float ylo, yhi, xlo, xhi, zlo, zhi, damping, offset;
     int hasCeiling;

@@ -25,6 +25,15 @@
 #include "sphx_common.h"
 #include "sphx_kernels.h"
 
+// Minimum resident CTAs of 256 threads per SM for the two walk kernels
+// (caps their registers at 65536 / (256 * N)).
+#ifndef SPHX_DENSITY_MIN_BLOCKS
+#define SPHX_DENSITY_MIN_BLOCKS 4
+#endif
+#ifndef SPHX_FORCE_MIN_BLOCKS
+#define SPHX_FORCE_MIN_BLOCKS 4
+#endif
+
 namespace sphx {
 namespace {
 
@@ -66,6 +75,9 @@ __global__ void k_keys(StepParams P, const float4 *__restrict__ pos, uint32_t *_
     if (in_domain(c.qx) && in_domain(c.qy) && in_domain(c.qz)) {
         int mx, my, mz;
         k = slot_of(P.grid, c.cx, c.cy, c.cz, mx, my, mz);
+        // a cell outside the grid's x extent shares its slot with a cell gx
+        // away: rows are then no longer sorted by x across their cells
+        if ((unsigned)(c.cx - P.grid.ox) >= (unsigned)P.grid.gx) status[1] = 1u;
     } else {
         atomicOr(status, kStatusDomainBit);
     }
@@ -184,19 +196,26 @@ __global__ void k_scatter(uint32_t n, const uint32_t *__restrict__ key,
     order[start[key[i]] + rank[i]] = i;
 }
 
-// The particle that arrived first in a cell sorts the cell's run ascending.
-__global__ void k_cellsort(uint32_t n, const uint32_t *__restrict__ key,
-                           const uint32_t *__restrict__ rank, const uint32_t *__restrict__ start,
-                           uint32_t *__restrict__ order, const uint32_t *__restrict__ status) {
+// The particle that arrived first in a cell sorts the cell's run by
+// (x, particle index): deterministic, and it makes every run of
+// x-consecutive cells sorted by x, which the walk's x window relies on.
+__global__ void k_cellsort(uint32_t n, const float4 *__restrict__ pos,
+                           const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
+                           const uint32_t *__restrict__ start, uint32_t *__restrict__ order,
+                           const uint32_t *__restrict__ status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || rank[i] != 0u || (*status & kStatusOverflowBit)) return;
     const uint32_t k = key[i];
     const uint32_t a = start[k], b = start[k + 1];
     for (uint32_t x = a + 1; x < b; ++x) {
         const uint32_t v = order[x];
+        const float vx = pos[v].x;
         uint32_t y = x;
-        while (y > a && order[y - 1] > v) {
-            order[y] = order[y - 1];
+        while (y > a) {
+            const uint32_t u = order[y - 1];
+            const float ux = pos[u].x;
+            if (!(ux > vx || (ux == vx && u > v))) break;
+            order[y] = u;
             --y;
         }
         order[y] = v;
@@ -224,25 +243,68 @@ struct WalkCtx {
     const uint32_t *__restrict__ start;
     Grid grid;
     float h2;
+    float hx;  // x half-width of the row window: h (1 + 2^-20)
+    bool xmono;  // every particle inside the grid's x extent this step
 };
 
 // One run of cell-sorted slots [a, b): every particle j != self with
 // |pj - pi|^2 < h^2 (reference's float r^2, sph.cpp:57: (dx*dx + dy*dy) + dz*dz,
 // no fused multiply-add) is passed to the visitor `w` times.
+template <class V>
+__device__ __forceinline__ void test_pair(const WalkCtx &W, uint32_t j, float4 pj, uint32_t self,
+                                          float4 pi, uint32_t w, V &vis) {
+    const float dx = __fsub_rn(pj.x, pi.x);
+    const float dy = __fsub_rn(pj.y, pi.y);
+    const float dz = __fsub_rn(pj.z, pi.z);
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    if (d2 < W.h2 && j != self)
+        for (uint32_t r = 0; r < w; ++r) vis(j, dx, dy, dz, d2);
+}
+
+// Two candidates are loaded per iteration so that their loads overlap.
 template <bool kInd, class V>
 __device__ __forceinline__ void scan_run(const WalkCtx &W, uint32_t a, uint32_t b, uint32_t self,
                                          float4 pi, uint32_t w, V &vis) {
-    for (uint32_t t = a; t < b; ++t) {
+    uint32_t t = a;
+    for (; t + 1 < b; t += 2) {
+        const uint32_t j0 = kInd ? W.order[t] : t;
+        const uint32_t j1 = kInd ? W.order[t + 1] : t + 1;
+        const float4 p0 = W.pos[j0];
+        const float4 p1 = W.pos[j1];
+        test_pair(W, j0, p0, self, pi, w, vis);
+        test_pair(W, j1, p1, self, pi, w, vis);
+    }
+    if (t < b) {
         const uint32_t j = kInd ? W.order[t] : t;
-        if (j == self) continue;
-        const float4 pj = W.pos[j];
-        const float dx = __fsub_rn(pj.x, pi.x);
-        const float dy = __fsub_rn(pj.y, pi.y);
-        const float dz = __fsub_rn(pj.z, pi.z);
-        const float d2 =
-            __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-        if (d2 < W.h2)
-            for (uint32_t r = 0; r < w; ++r) vis(j, dx, dy, dz, d2);
+        test_pair(W, j, W.pos[j], self, pi, w, vis);
+    }
+}
+
+// As scan_run, over a run sorted by x, visiting only candidates whose x lies
+// in [xlo, xhi]: the run is entered at its first x >= xlo and left at the
+// first x > xhi.  Any j with float r^2 < h^2 has |xj - xi| < h (1 + 2^-22),
+// so a window of half-width h (1 + 2^-20) plus rounding slack loses none.
+// When some particle lies outside the grid's x extent (xmono false) the run
+// is not monotone in x and candidates past xhi are skipped, not the rest of
+// the run.
+template <bool kInd, class V>
+__device__ __forceinline__ void scan_run_x(const WalkCtx &W, uint32_t a, uint32_t b, uint32_t self,
+                                           float4 pi, float xlo, float xhi, bool xmono, V &vis) {
+    uint32_t t = a;
+    for (; t + 1 < b; t += 2) {
+        const uint32_t j0 = kInd ? W.order[t] : t;
+        const uint32_t j1 = kInd ? W.order[t + 1] : t + 1;
+        const float4 p0 = W.pos[j0];
+        const float4 p1 = W.pos[j1];
+        if (xmono && p0.x > xhi) return;
+        if (p0.x >= xlo && p0.x <= xhi) test_pair(W, j0, p0, self, pi, 1u, vis);
+        if (xmono && p1.x > xhi) return;
+        if (p1.x >= xlo && p1.x <= xhi) test_pair(W, j1, p1, self, pi, 1u, vis);
+    }
+    if (t < b) {
+        const uint32_t j = kInd ? W.order[t] : t;
+        const float4 p = W.pos[j];
+        if (p.x >= xlo && p.x <= xhi) test_pair(W, j, p, self, pi, 1u, vis);
     }
 }
 
@@ -252,26 +314,42 @@ __device__ __forceinline__ int wrap1(int v, int m) {
 }
 
 // Fast path: the 27 cells around (mx, my, mz), each visited once.
+__device__ __forceinline__ uint32_t row_base(const Grid &g, int my, int mz, int r) {
+    const int z = wrap1(mz + r / 3 - 1, g.gz);
+    const int y = wrap1(my + r % 3 - 1, g.gy);
+    return ((uint32_t)z * (uint32_t)g.gy + (uint32_t)y) * (uint32_t)g.gx;
+}
+
+// Fast path: the 27 cells around (mx, my, mz), each visited once.  With the
+// particle's slot away from the grid's x seam, each (dy, dz) row of three
+// cells is one contiguous run; the bounds of row r+1 are loaded before row r
+// is scanned.
 template <bool kInd, class V>
 __device__ __forceinline__ void walk_rows(const WalkCtx &W, int mx, int my, int mz, uint32_t self,
                                           float4 pi, V &vis) {
     const Grid &g = W.grid;
-    const bool contiguous = mx >= 1 && mx + 1 < g.gx;
+    if (mx >= 1 && mx + 1 < g.gx) {
+        const float hx = fmaf(fabsf(pi.x), 2.384185791015625e-07f, W.hx);  // + |x| 2^-22
+        const float xlo = pi.x - hx, xhi = pi.x + hx;
+        uint32_t base = row_base(g, my, mz, 0);
+        uint32_t a = W.start[base + mx - 1], b = W.start[base + mx + 2];
 #pragma unroll 1
-    for (int dz = -1; dz <= 1; ++dz) {
-        const int z = wrap1(mz + dz, g.gz);
+        for (int r = 0; r < 9; ++r) {
+            const uint32_t ca = a, cb = b;
+            if (r < 8) {
+                base = row_base(g, my, mz, r + 1);
+                a = W.start[base + mx - 1];
+                b = W.start[base + mx + 2];
+            }
+            scan_run_x<kInd>(W, ca, cb, self, pi, xlo, xhi, W.xmono, vis);
+        }
+    } else {
 #pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int y = wrap1(my + dy, g.gy);
-            const uint32_t base = ((uint32_t)z * (uint32_t)g.gy + (uint32_t)y) * (uint32_t)g.gx;
-            if (contiguous) {
-                scan_run<kInd>(W, W.start[base + mx - 1], W.start[base + mx + 2], self, pi, 1u,
-                               vis);
-            } else {
-                for (int dx = -1; dx <= 1; ++dx) {
-                    const uint32_t k = base + (uint32_t)wrap1(mx + dx, g.gx);
-                    scan_run<kInd>(W, W.start[k], W.start[k + 1], self, pi, 1u, vis);
-                }
+        for (int r = 0; r < 9; ++r) {
+            const uint32_t base = row_base(g, my, mz, r);
+            for (int dx = -1; dx <= 1; ++dx) {
+                const uint32_t k = base + (uint32_t)wrap1(mx + dx, g.gx);
+                scan_run<kInd>(W, W.start[k], W.start[k + 1], self, pi, 1u, vis);
             }
         }
     }
@@ -375,10 +453,11 @@ struct DensityVisitor {
 // here the cubes are summed and scaled once (the two differ by float
 // rounding only).
 template <bool kInd>
-__global__ void __launch_bounds__(256) k_density(StepParams P, WalkCtx W, float2 *__restrict__ rp,
+__global__ void __launch_bounds__(256, SPHX_DENSITY_MIN_BLOCKS) k_density(StepParams P, WalkCtx W, float4 *__restrict__ rp,
                                                  const uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n || *status) return;
+    if (t >= P.n || (status[0] & kStatusErrorMask)) return;
+    W.xmono = status[1] == 0u;
     const uint32_t i = kInd ? W.order[t] : t;
     const float4 pi = W.pos[i];
     WalkStart s;
@@ -387,46 +466,69 @@ __global__ void __launch_bounds__(256) k_density(StepParams P, WalkCtx W, float2
     walk<kInd>(W, s, i, pi, v);
     const float rho = __fadd_rn(__fmul_rn(P.mp6, v.acc), P.selfDens);
     const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
-    rp[i] = make_float2(rho, prs);
+    rp[i] = make_float4(rho, prs, __frcp_rn(rho), 0.f);
 }
 
-// One accepted pair of sph.cpp:107-121, operation for operation in FP32
-// without fused multiply-adds.
-struct ForceVisitor {
+// One accepted pair of sph.cpp:107-121.  With d = pj - pi, r = |d| and
+// hd = h - r, the reference's two terms are
+//   pressure   -(d / r) * m * (pi + pj) / (2 rho_j) * spikyGrad * hd^2
+//   viscosity  mu * m * (vj - vi) / rho_j * spikyLap * hd
+// evaluated here as -cp * d + cv * (vj - vi) with cp = kp (pi + pj) hd^2 / (rho_j r),
+// kp = m spikyGrad / 2, and cv = kv hd / rho_j, kv = mu m spikyLap: the same
+// products without divisions (1/rho_j comes precomputed with the density).
+// Per term this moves the result by a few float ulps; summed forces stay
+// within about 1e-6 of the reference's (rms-floored relative metric).
+struct ForcePair {
     const float4 *__restrict__ vel;
-    const float2 *__restrict__ rp;
+    const float4 *__restrict__ rp;
     float4 vi;
-    float presI, h, mass, mm, spikyGrad, spikyLap;
+    float presI, h, kp, kv;
     float fx, fy, fz;
     float cx, cy, cz;  // Kahan compensations
     __device__ __forceinline__ void operator()(uint32_t j, float dx, float dy, float dz, float d2) {
         const float4 vj = vel[j];
-        const float2 q = rp[j];
-        const float dist = __fsqrt_rn(d2);
-        const float inv = __fdiv_rn(1.f, dist);  // normalize: d * (1 / sqrt(dot(d, d)))
-        const float nx = __fmul_rn(dx, inv), ny = __fmul_rn(dy, inv), nz = __fmul_rn(dz, inv);
-        const float psum = __fadd_rn(presI, q.y);
-        const float twoRho = __fmul_rn(2.f, q.x);
-        const float hd = __fsub_rn(h, dist);
-        const float sq = __fmul_rn(hd, hd);  // (float)pow(double(h - dist), 2)
-        const float px = __fmul_rn(
-            __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(-nx, mass), psum), twoRho), spikyGrad), sq);
-        const float py = __fmul_rn(
-            __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(-ny, mass), psum), twoRho), spikyGrad), sq);
-        const float pz = __fmul_rn(
-            __fmul_rn(__fdiv_rn(__fmul_rn(__fmul_rn(-nz, mass), psum), twoRho), spikyGrad), sq);
-        kahan_add(fx, cx, px);
-        kahan_add(fy, cy, py);
-        kahan_add(fz, cz, pz);
-        const float vx =
-            __fmul_rn(__fmul_rn(__fmul_rn(mm, __fdiv_rn(__fsub_rn(vj.x, vi.x), q.x)), spikyLap), hd);
-        const float vy =
-            __fmul_rn(__fmul_rn(__fmul_rn(mm, __fdiv_rn(__fsub_rn(vj.y, vi.y), q.x)), spikyLap), hd);
-        const float vz =
-            __fmul_rn(__fmul_rn(__fmul_rn(mm, __fdiv_rn(__fsub_rn(vj.z, vi.z), q.x)), spikyLap), hd);
-        kahan_add(fx, cx, vx);
-        kahan_add(fy, cy, vy);
-        kahan_add(fz, cz, vz);
+        const float4 q = rp[j];
+        const float invr = rsqrtf(d2);
+        const float r = d2 * invr;
+        const float hd = h - r;
+        const float cp = kp * (presI + q.y) * q.z * (hd * hd) * invr;
+        const float cv = kv * hd * q.z;
+        kahan_add(fx, cx, fmaf(cv, vj.x - vi.x, -cp * dx));
+        kahan_add(fy, cy, fmaf(cv, vj.y - vi.y, -cp * dy));
+        kahan_add(fz, cz, fmaf(cv, vj.z - vi.z, -cp * dz));
+    }
+};
+
+// The force walk in two phases: the candidate test only appends accepted
+// neighbours to this thread's column of a shared-memory list; the pair
+// math then runs over the list with every lane busy, instead of under the
+// acceptance branch (about 1 candidate in 4 passes) with most lanes idle.
+constexpr int kForceThreads = 256;
+constexpr int kForceList = 48;  // list slots per thread (flushed when full)
+
+struct ForceListVisitor {
+    uint32_t *list;  // this thread's column: list[k * kForceThreads]
+    uint32_t cnt;
+    const float4 *__restrict__ pos;
+    float4 pi;
+    ForcePair pair;
+    __device__ __forceinline__ void flush() {
+#pragma unroll 1
+        for (uint32_t k = 0; k < cnt; ++k) {
+            const uint32_t j = list[k * kForceThreads];
+            const float4 pj = pos[j];
+            const float dx = __fsub_rn(pj.x, pi.x);
+            const float dy = __fsub_rn(pj.y, pi.y);
+            const float dz = __fsub_rn(pj.z, pi.z);
+            const float d2 =
+                __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            pair(j, dx, dy, dz, d2);
+        }
+        cnt = 0;
+    }
+    __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float) {
+        list[cnt * kForceThreads] = j;
+        if (++cnt == (uint32_t)kForceList) flush();
     }
 };
 
@@ -471,23 +573,28 @@ __device__ __forceinline__ void integrate(const StepParams &P, float4 &x, float4
 }
 
 template <bool kInd>
-__global__ void __launch_bounds__(256)
-    k_force(StepParams P, WalkCtx W, const float4 *__restrict__ vel, const float2 *__restrict__ rp,
+__global__ void __launch_bounds__(kForceThreads, SPHX_FORCE_MIN_BLOCKS)
+    k_force(StepParams P, WalkCtx W, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
             float4 *__restrict__ force_out, const uint32_t *__restrict__ status) {
+    __shared__ uint32_t s_list[kForceList * kForceThreads];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n || *status) return;
+    if (t >= P.n || (status[0] & kStatusErrorMask)) return;
+    W.xmono = status[1] == 0u;
     const uint32_t i = kInd ? W.order[t] : t;
     float4 pi = W.pos[i];
     float4 vi = vel[i];
-    const float2 q = rp[i];
+    const float4 q = rp[i];
     WalkStart s;
     walk_start(P, pi, s);
-    ForceVisitor v{vel,    rp,      vi, q.y, P.h, P.mass, __fmul_rn(P.viscosity, P.mass),
-                   P.spikyGrad, P.spikyLap, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    ForceListVisitor v{s_list + threadIdx.x, 0u, W.pos, pi,
+                       ForcePair{vel, rp, vi, q.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f,
+                                 0.f, 0.f}};
     walk<kInd>(W, s, i, pi, v);
-    force_out[i] = make_float4(v.fx, v.fy, v.fz, 0.f);
-    integrate(P, pi, vi, v.fx, v.fy, v.fz, q.x);
+    v.flush();
+    const float fx = v.pair.fx, fy = v.pair.fy, fz = v.pair.fz;
+    force_out[i] = make_float4(fx, fy, fz, 0.f);
+    integrate(P, pi, vi, fx, fy, fz, q.x);
     pos_out[i] = pi;
     vel_out[i] = vi;
 }
@@ -516,7 +623,8 @@ __global__ void k_digest(StepParams P, WalkCtx W, const uint32_t *__restrict__ i
                          uint32_t *__restrict__ count_out, uint64_t *__restrict__ digest_out,
                          const uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n || *status) return;
+    if (t >= P.n || (status[0] & kStatusErrorMask)) return;
+    W.xmono = status[1] == 0u;
     const uint32_t i = kInd ? W.order[t] : t;
     const float4 pi = W.pos[i];
     WalkStart s;
@@ -541,7 +649,7 @@ __global__ void k_upload(uint32_t n, const float *__restrict__ pos3, const float
 // Field readout in id order: 3 floats per particle for vec fields, 1 for
 // scalars.  field: 0 pos, 1 vel, 2 force, 3 rho, 4 prs.
 __global__ void k_read_field(uint32_t n, int field, const uint32_t *__restrict__ id,
-                             const float4 *__restrict__ v4, const float2 *__restrict__ rp,
+                             const float4 *__restrict__ v4, const float4 *__restrict__ rp,
                              float *__restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -552,7 +660,7 @@ __global__ void k_read_field(uint32_t n, int field, const uint32_t *__restrict__
         out[3 * d + 1] = v.y;
         out[3 * d + 2] = v.z;
     } else {
-        const float2 q = rp[i];
+        const float4 q = rp[i];
         out[d] = field == 3 ? q.x : q.y;
     }
 }
@@ -588,6 +696,62 @@ __global__ void k_cells(uint32_t n, float h, const uint32_t *__restrict__ id,
     if (hash) hash[d] = (uint16_t)hash16(c.cx, c.cy, c.cz);
 }
 
+// The reference's 60-byte Particle record (Particle.h:4-10): four vec3, two
+// floats and the uint16 hash (plus 2 bytes of tail padding).
+struct ParticleRec {
+    float pos[3], vel[3], acc[3], force[3];
+    float density, pressure;
+    uint16_t hash;
+    uint16_t pad;
+};
+static_assert(sizeof(ParticleRec) == 60, "Particle layout");
+
+// AoS -> resident SoA (id = record index).  hash_pre keeps hash16 of each
+// record's pre-step cell, which the reference's GPU path leaves in the
+// record (sphGPU.cu:31-40 runs before the positions move).
+__global__ void k_aos_unpack(uint32_t n, float h, const ParticleRec *__restrict__ rec,
+                             float4 *__restrict__ pos, float4 *__restrict__ vel,
+                             uint32_t *__restrict__ id, uint16_t *__restrict__ hash_pre) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const ParticleRec &r = rec[i];
+    const float4 p = make_float4(r.pos[0], r.pos[1], r.pos[2], 0.f);
+    pos[i] = p;
+    vel[i] = make_float4(r.vel[0], r.vel[1], r.vel[2], 0.f);
+    id[i] = i;
+    const CellPos c = cell_pos(p, h);
+    hash_pre[i] = (uint16_t)hash16(c.cx, c.cy, c.cz);
+}
+
+// Resident SoA -> AoS records in the caller's order, plus the instanced
+// renderer's transforms; `acceleration` (never written by the reference) is
+// left as the caller passed it.
+__global__ void k_aos_pack(uint32_t n, float half_h, ParticleRec *__restrict__ rec,
+                           const uint32_t *__restrict__ id, const float4 *__restrict__ pos,
+                           const float4 *__restrict__ vel, const float4 *__restrict__ force,
+                           const float4 *__restrict__ rp, const uint16_t *__restrict__ hash_pre,
+                           float4 *__restrict__ transforms) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t d = id[i];
+    ParticleRec &r = rec[d];
+    const float4 p = pos[i], v = vel[i], f = force[i];
+    const float4 q = rp[i];
+    r.pos[0] = p.x; r.pos[1] = p.y; r.pos[2] = p.z;
+    r.vel[0] = v.x; r.vel[1] = v.y; r.vel[2] = v.z;
+    r.force[0] = f.x; r.force[1] = f.y; r.force[2] = f.z;
+    r.density = q.x;
+    r.pressure = q.y;
+    r.hash = hash_pre[d];
+    if (transforms) {
+        float4 *m = transforms + 4 * (size_t)d;
+        m[0] = make_float4(half_h, 0.f, 0.f, 0.f);
+        m[1] = make_float4(0.f, half_h, 0.f, 0.f);
+        m[2] = make_float4(0.f, 0.f, half_h, 0.f);
+        m[3] = make_float4(__fadd_rn(p.x, 0.f), __fadd_rn(p.y, 0.f), __fadd_rn(p.z, 0.f), 1.f);
+    }
+}
+
 inline unsigned blocks(uint32_t n, unsigned bs) { return (n + bs - 1) / bs; }
 
 }  // namespace
@@ -600,13 +764,14 @@ cudaError_t launch_sort(const StepParams &P, const SortBuffers &B, const float4 
     const uint32_t n = P.n;
     const uint32_t m = B.slots + 1;  // count[slots] stays 0 -> start[slots] = n
     const uint32_t ntiles = (m + kScanTile - 1) / kScanTile;
+    cudaMemsetAsync(B.status + 1, 0, 4, st);
     if (n) k_keys<<<blocks(n, bs), bs, 0, st>>>(P, pos, B.key, B.rank, B.count, B.status);
     k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.max_cell, B.status);
     k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(B.tile_sum, ntiles);
     k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.start);
     if (n) {
         k_scatter<<<blocks(n, bs), bs, 0, st>>>(n, B.key, B.rank, B.start, B.order, B.status);
-        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, B.key, B.rank, B.start, B.order, B.status);
+        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.order, B.status);
     }
     return cudaGetLastError();
 }
@@ -626,11 +791,13 @@ static WalkCtx make_ctx(const StepParams &P, const SortBuffers &B, const float4 
     W.start = B.start;
     W.grid = P.grid;
     W.h2 = P.h2;
+    W.hx = P.h * (1.0f + 9.5367431640625e-07f);
+    W.xmono = true;
     return W;
 }
 
 cudaError_t launch_density(const StepParams &P, const SortBuffers &B, const float4 *pos,
-                           float2 *rp, bool indirect, cudaStream_t st) {
+                           float4 *rp, bool indirect, cudaStream_t st) {
     const WalkCtx W = make_ctx(P, B, pos);
     if (P.n) {
         if (indirect) k_density<true><<<blocks(P.n, 256), 256, 0, st>>>(P, W, rp, B.status);
@@ -640,16 +807,16 @@ cudaError_t launch_density(const StepParams &P, const SortBuffers &B, const floa
 }
 
 cudaError_t launch_force(const StepParams &P, const SortBuffers &B, const float4 *pos,
-                         const float4 *vel, const float2 *rp, float4 *pos_out, float4 *vel_out,
+                         const float4 *vel, const float4 *rp, float4 *pos_out, float4 *vel_out,
                          float4 *force_out, bool indirect, cudaStream_t st) {
     const WalkCtx W = make_ctx(P, B, pos);
     if (P.n) {
         if (indirect)
-            k_force<true><<<blocks(P.n, 256), 256, 0, st>>>(P, W, vel, rp, pos_out, vel_out,
-                                                            force_out, B.status);
+            k_force<true><<<blocks(P.n, kForceThreads), kForceThreads, 0, st>>>(
+                P, W, vel, rp, pos_out, vel_out, force_out, B.status);
         else
-            k_force<false><<<blocks(P.n, 256), 256, 0, st>>>(P, W, vel, rp, pos_out, vel_out,
-                                                             force_out, B.status);
+            k_force<false><<<blocks(P.n, kForceThreads), kForceThreads, 0, st>>>(
+                P, W, vel, rp, pos_out, vel_out, force_out, B.status);
     }
     return cudaGetLastError();
 }
@@ -674,7 +841,7 @@ cudaError_t launch_upload(uint32_t n, const float *pos3, const float *vel3, floa
 }
 
 cudaError_t launch_read_field(uint32_t n, int field, const uint32_t *id, const float4 *v4,
-                              const float2 *rp, float *out, cudaStream_t st) {
+                              const float4 *rp, float *out, cudaStream_t st) {
     if (n) k_read_field<<<blocks(n, 256), 256, 0, st>>>(n, field, id, v4, rp, out);
     return cudaGetLastError();
 }
@@ -690,6 +857,25 @@ cudaError_t launch_transforms(uint32_t n, float half_h, const uint32_t *id, cons
 cudaError_t launch_cells(uint32_t n, float h, const uint32_t *id, const float4 *pos, int *cells,
                          uint16_t *hash, cudaStream_t st) {
     if (n) k_cells<<<blocks(n, 256), 256, 0, st>>>(n, h, id, pos, cells, hash);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aos_unpack(uint32_t n, float h, const void *rec, float4 *pos, float4 *vel,
+                              uint32_t *id, uint16_t *hash_pre, cudaStream_t st) {
+    if (n)
+        k_aos_unpack<<<blocks(n, 256), 256, 0, st>>>(n, h, static_cast<const ParticleRec *>(rec),
+                                                     pos, vel, id, hash_pre);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_aos_pack(uint32_t n, float half_h, void *rec, const uint32_t *id,
+                            const float4 *pos, const float4 *vel, const float4 *force,
+                            const float4 *rp, const uint16_t *hash_pre, float *transforms16,
+                            cudaStream_t st) {
+    if (n)
+        k_aos_pack<<<blocks(n, 256), 256, 0, st>>>(n, half_h, static_cast<ParticleRec *>(rec), id,
+                                                   pos, vel, force, rp, hash_pre,
+                                                   reinterpret_cast<float4 *>(transforms16));
     return cudaGetLastError();
 }
 

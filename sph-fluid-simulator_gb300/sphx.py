@@ -111,6 +111,8 @@ def lib():
         "sphx_read_cells": (C.c_int, [vp, vp, vp]),
         "sphx_neighbor_digest": (C.c_int, [vp, vp, vp]),
         "sphx_device_state": (C.c_int, [vp, P(DeviceView)]),
+        "sphx_update_particles": (C.c_int, [vp, vp, C.c_size_t, P(Settings), P(Box), C.c_float]),
+        "sphx_update_particles_release": (C.c_int, []),
         "sphx_set_profiling": (C.c_int, [vp, C.c_int]),
         "sphx_get_kernel_times": (C.c_int, [vp, P(KernelTimes)]),
     }
@@ -227,6 +229,36 @@ def dambreak(nx, ny=None, nz=None, box_scale=(2.5, 1.25, 1.25), box_dims=None, s
     origin = (b.xmin + h + spacing, b.ymin + h + spacing, b.zmin + h + spacing)
     pos = lattice(nx, ny, nz, origin, spacing, jitter, seed)
     return pos, b
+
+
+# ------------------------------------------------------------------ reference seam
+
+PARTICLE_DTYPE = np.dtype([("position", np.float32, 3), ("velocity", np.float32, 3),
+                           ("acceleration", np.float32, 3), ("force", np.float32, 3),
+                           ("density", np.float32), ("pressure", np.float32),
+                           ("hash", np.uint16), ("_pad", np.uint16)])
+assert PARTICLE_DTYPE.itemsize == 60  # Particle.h:4-10
+
+
+def particles_from(pos, vel=None):
+    """An array of the reference's 60-byte Particle records."""
+    rec = np.zeros(len(pos), PARTICLE_DTYPE)
+    rec["position"] = pos
+    if vel is not None:
+        rec["velocity"] = vel
+    return rec
+
+
+def update_particles(records, s, dt, box=None, transforms=None):
+    """One step in place over Particle records (updateParticlesGPU's contract)."""
+    assert records.dtype == PARTICLE_DTYPE and records.flags["C_CONTIGUOUS"]
+    _check(lib().sphx_update_particles(C.c_void_p(records.ctypes.data),
+                                       _ptr(transforms), len(records), C.byref(s),
+                                       C.byref(box) if box is not None else None, dt))
+
+
+def release_update_particles():
+    _check(lib().sphx_update_particles_release())
 
 
 # ------------------------------------------------------------------ scene handle
