@@ -172,6 +172,21 @@ int sphx_update_particles(void *particles, float *transforms16, size_t n,
 /* Frees the state cached by sphx_update_particles. */
 int sphx_update_particles_release(void);
 
+/* No counterpart in the reference.  Density and pressure (the values one
+ * step would compute, src/sph.cpp:28-76) of n particles whose positions are
+ * already on the device (d_pos4: n float4 rows x, y, z, unused), written to
+ * the caller's device arrays d_rho and d_prs, on `stream` (NULL: the default
+ * stream), without allocating any memory: for callers that cannot allocate
+ * device memory when they need the result (a plugin inside a frame with a
+ * fixed GPU memory budget, or a host that gives the library buffers but no
+ * right to call cudaMalloc).  Its scratch is one static device array of about
+ * 5.5 MiB per GPU, held until the process exits; n may be at most 131,072
+ * (larger n: SPHX_ERR_INVALID).  Calls share that array, so calls whose work
+ * overlaps on the GPU race.  The first call on a device looks up the array's
+ * address; make it before any stream capture.  Synchronises `stream`. */
+int sphx_density_static(const sphx_settings *s, const void *d_pos4, size_t n, float *d_rho,
+                        float *d_prs, void *stream);
+
 int sphx_set_profiling(sphx_handle *h, int enable);
 /* Synchronises, then returns the accumulated per-phase times and resets them. */
 int sphx_get_kernel_times(sphx_handle *h, sphx_kernel_times *out);

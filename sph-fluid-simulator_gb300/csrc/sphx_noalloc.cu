@@ -1,0 +1,147 @@
+// sphx_density_static: density and pressure of caller-owned device positions
+// without allocating anything.
+//
+// Some callers of this library cannot allocate device memory when they need
+// a result: a render or game-engine plugin that runs inside a frame with a
+// fixed GPU memory budget, or a host that hands the library device buffers
+// but does not let it call cudaMalloc (or any allocating routine) on its
+// behalf.  For them this entry point keeps every scratch buffer the density
+// pass needs (sort keys, ranks, cell order, the cell-grid counts and starts,
+// scan tile sums, the status word and the per-particle (rho, p, 1/rho)
+// record) in one file-scope __device__ array of fixed size.  The caller
+// passes the inputs (positions) and outputs (density, pressure) as device
+// pointers; nothing is allocated or freed, by this code or by a library it
+// calls.
+//
+// Limits and sharing:
+//   * at most kMaxParticles (131,072) particles per call; more is rejected
+//     with SPHX_ERR_INVALID;
+//   * the array (about 5.5 MiB) lives in every GPU that loads the library
+//     until the process exits;
+//   * every call on a device uses the same array, which keeps the previous
+//     call's contents: the counts and status words are cleared at the start
+//     of each call, and two calls whose work overlaps on the GPU race on the
+//     array (serialise them, e.g. on one stream);
+//   * the first call on a device looks up the array's device address
+//     (cudaGetSymbolAddress) with that device current and caches it; make
+//     that first call before any stream capture.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include "sphx_internal.h"
+
+namespace {
+
+constexpr uint32_t kMaxParticles = 1u << 17;
+constexpr int kGridDim = 64;  // modular 64^3 cell grid: exact for any extent (aliasing only slows)
+constexpr int kGridOrigin = -32;  // cells -32..31 on each axis map without wrapping
+constexpr uint32_t kSlots = (uint32_t)kGridDim * kGridDim * kGridDim;
+constexpr uint32_t kTiles = (kSlots + 1 + 4095) / 4096;
+constexpr int kMaxDevices = 64;
+
+// Byte offsets of the scratch buffers inside the array (all 256-aligned).
+constexpr size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+constexpr size_t kOffKey = 0;
+constexpr size_t kOffRank = kOffKey + align256(4ull * kMaxParticles);
+constexpr size_t kOffOrder = kOffRank + align256(4ull * kMaxParticles);
+constexpr size_t kOffCount = kOffOrder + align256(4ull * kMaxParticles);
+constexpr size_t kOffStart = kOffCount + align256(4ull * (kSlots + 1));
+constexpr size_t kOffTiles = kOffStart + align256(4ull * (kSlots + 1));
+constexpr size_t kOffStatus = kOffTiles + align256(4ull * kTiles);
+constexpr size_t kOffRp = kOffStatus + 256;
+constexpr size_t kScratchBytes = kOffRp + 16ull * kMaxParticles;
+
+static __device__ __align__(256) uint4 g_scratch[kScratchBytes / sizeof(uint4)];
+
+std::mutex g_mu;
+char *g_addr[kMaxDevices] = {};
+
+// Device address of g_scratch on the current device (looked up once).
+int scratch_address(char **out) {
+    int dev = 0;
+    SPHX_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return sphx::fail(SPHX_ERR_CUDA, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+        if (e != cudaSuccess)
+            return sphx::fail(SPHX_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_addr[dev] = static_cast<char *>(p);
+    }
+    *out = g_addr[dev];
+    return SPHX_OK;
+}
+
+__global__ void k_split_rho_prs(uint32_t n, const float4 *__restrict__ rp, float *__restrict__ rho,
+                                float *__restrict__ prs) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 q = rp[i];
+    rho[i] = q.x;
+    prs[i] = q.y;
+}
+
+}  // namespace
+
+extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, size_t n,
+                                   float *d_rho, float *d_prs, void *stream) {
+    using sphx::fail;
+    if (!s || !d_pos4 || !d_rho || !d_prs) return fail(SPHX_ERR_INVALID, "null argument");
+    if (n == 0 || n > kMaxParticles)
+        return fail(SPHX_ERR_INVALID, "sphx_density_static: particle count " + std::to_string(n) +
+                                          " outside [1, " + std::to_string(kMaxParticles) +
+                                          "], the size of its static scratch");
+    if (!(s->h > 0.f) || !std::isfinite(s->h)) return fail(SPHX_ERR_INVALID, "h must be finite and > 0");
+    char *base = nullptr;
+    int rc = scratch_address(&base);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    const sphx::Derived d = sphx::derive_constants(s->mass, s->rest_density, s->gas_const,
+                                                   s->viscosity, s->h, s->g, s->tension);
+    sphx::StepParams P{};
+    P.h = d.h;
+    P.h2 = d.h2;
+    P.mp6 = d.massPoly6Product;
+    P.selfDens = d.selfDens;
+    P.gasConstant = d.gasConstant;
+    P.restDensity = d.restDensity;
+    P.mass = d.mass;
+    P.grid = sphx::Grid{kGridOrigin, kGridOrigin, kGridOrigin, kGridDim, kGridDim, kGridDim};
+    P.n = (uint32_t)n;
+
+    sphx::SortBuffers B;
+    B.key = reinterpret_cast<uint32_t *>(base + kOffKey);
+    B.rank = reinterpret_cast<uint32_t *>(base + kOffRank);
+    B.order = reinterpret_cast<uint32_t *>(base + kOffOrder);
+    B.count = reinterpret_cast<uint32_t *>(base + kOffCount);
+    B.start = reinterpret_cast<uint32_t *>(base + kOffStart);
+    B.tile_sum = reinterpret_cast<uint32_t *>(base + kOffTiles);
+    B.status = reinterpret_cast<uint32_t *>(base + kOffStatus);
+    B.slots = kSlots;
+    B.max_cell = 1024;
+    float4 *rp = reinterpret_cast<float4 *>(base + kOffRp);
+    const float4 *pos = static_cast<const float4 *>(d_pos4);
+
+    // The previous call's contents stay in the array: counts and status
+    // must start from zero.
+    SPHX_CUDA(cudaMemsetAsync(B.count, 0, 4ull * (kSlots + 1), st));
+    SPHX_CUDA(cudaMemsetAsync(B.status, 0, 16, st));
+    SPHX_CUDA(sphx::launch_sort(P, B, pos, st));
+    SPHX_CUDA(sphx::launch_density(P, B, pos, rp, /*indirect=*/true, st));
+    k_split_rho_prs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P.n, rp, d_rho, d_prs);
+    SPHX_CUDA(cudaGetLastError());
+
+    uint32_t status = 0;
+    SPHX_CUDA(cudaMemcpyAsync(&status, B.status, 4, cudaMemcpyDeviceToHost, st));
+    SPHX_CUDA(cudaStreamSynchronize(st));
+    if (status & sphx::kStatusDomainBit)
+        return fail(SPHX_ERR_DOMAIN, "a position is non-finite or |x/h| >= 2^30");
+    if (status & sphx::kStatusOverflowBit)
+        return fail(SPHX_ERR_OVERFLOW, "a cell holds more than 1024 particles");
+    return SPHX_OK;
+}
