@@ -48,6 +48,19 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(x):
+    """Max of a float over all ranks (identity when not distributed).  Uses a
+    CUDA tensor under NCCL and a CPU tensor under gloo."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -69,7 +82,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -130,6 +143,143 @@ def cpu_baseline(pos, box, s, budget_s=15.0, max_steps=20):
             "sample": "%d steps of the %d-particle workload from its initial state "
                       "(oracle restatement of updateParticlesCPU, std::thread x %d)"
                       % (steps, len(pos), port.hw_threads())}
+
+
+def batch_compare(scenes, steps, warmup, device, cache_path=None):
+    """Scenes/s of the batched form against the same scenes one at a time
+    through the plain single-scene path, each arm end to end: upload, `steps`
+    steps of dt, readout of every scene (the batched arm's autotuning is a
+    one-off, cached, and not timed)."""
+    import torch
+    import sphx
+    opts = sphx.default_options(device=device)
+    with sphx.Scene.batch(scenes, opts) as b:
+        tune = b.autotune(sphx.DT, trial_steps=3, cache_path=cache_path)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    with sphx.Scene.batch(scenes, opts) as b:
+        b.set_tuning(tune.density_threads, tune.force_threads, tune.reorder_interval)
+        b.step(sphx.DT, steps)
+        for k in range(len(scenes)):
+            b.read_scene(k)
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for s, pos, box in scenes:
+        with sphx.Scene(s, box, pos, None, opts) as one:
+            one.step(sphx.DT, steps)
+            one.read()
+    t_seq = time.perf_counter() - t0
+    n = sum(len(p) for _, p, _ in scenes)
+    return {"scenes": len(scenes), "particles": n, "steps": steps,
+            "batched_scenes_per_s": len(scenes) / t_batch,
+            "sequential_scenes_per_s": len(scenes) / t_seq,
+            "speedup": t_seq / t_batch,
+            "batched_particle_steps_per_s": n * steps / t_batch,
+            "tuning": {"density_threads": tune.density_threads, "force_threads": tune.force_threads,
+                       "reorder_interval": tune.reorder_interval},
+            "note": "end to end per arm: upload, steps, readout; results bit-identical per scene"}
+
+
+def run_batch(a):
+    import torch
+    import sphx
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    scenes = sphx.batch_scenes(512, seed=0)
+    res = batch_compare(scenes, a.steps, a.warmup, local,
+                        cache_path=os.path.join(ROOT, "gpurun_out", "autotune.txt")
+                        if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None)
+    line = {"metric": "scenes/s (512 scenes, batched vs one at a time)", "value": res["batched_scenes_per_s"],
+            "unit": "scenes/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "512 dam-break scenes, N log-uniform [1000, 65536], aspect U[0.5,2], "
+                                   "k U[10,40], mu U[0.5,3], box 2.5/1.25/1.25 x block"},
+            "batched": res}
+    print(json.dumps(line), flush=True)
+
+
+def serve_requests(count, seed=1):
+    """The served workload's request stream: dam-break blocks with N
+    log-uniform in [2000, 500000], step counts uniform in [100, 2000], k and mu
+    drawn as in the batched workload."""
+    import math
+    import sphx
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(count):
+        target = math.exp(rng.uniform(math.log(2000), math.log(500000)))
+        aspect = rng.uniform(0.5, 2.0, 3)
+        c = (target / aspect.prod()) ** (1.0 / 3.0)
+        nx, ny, nz = (max(2, int(round(c * x))) for x in aspect)
+        s = sphx.config_settings(gas_const=float(rng.uniform(10, 40)),
+                                 viscosity=float(rng.uniform(0.5, 3)))
+        pos, box = sphx.dambreak(nx, ny, nz, seed=seed * 7919 + k)
+        reqs.append((s, pos, box, int(rng.integers(100, 2001))))
+    return reqs
+
+
+def run_serve(a):
+    """Poisson arrivals at each rate: p50/p95/p99 completion latency and
+    scenes/s of the continuous-batching server, against the same stream
+    served one request at a time through the plain path (FIFO: each request
+    starts when both it has arrived and the previous one has finished, with
+    its measured service time)."""
+    import torch
+    import sphx
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    reqs = serve_requests(a.requests, seed=1)
+    # service time of each request alone (plain path, end to end)
+    service = []
+    for s, pos, box, nsteps in reqs:
+        t0 = time.perf_counter()
+        with sphx.Scene(s, box, pos, None, sphx.default_options(device=local)) as one:
+            one.step(sphx.DT, nsteps)
+            one.read()
+        service.append(time.perf_counter() - t0)
+    results = []
+    rng = np.random.default_rng(2)
+    for lam in [float(x) for x in a.rates.split(",")]:
+        arrivals = np.cumsum(rng.exponential(1.0 / lam, len(reqs)))
+        arrivals -= arrivals[0]
+        # sequential plain FIFO
+        end = 0.0
+        lat_seq = []
+        for t_arr, svc in zip(arrivals, service):
+            start = max(t_arr, end)
+            end = start + svc
+            lat_seq.append(end - t_arr)
+        span_seq = end - arrivals[0]
+        # continuous batching
+        with sphx.Server(budget_bytes=150e9, steps_per_tick=a.tick, device=local) as srv:
+            t0 = time.perf_counter()
+            tickets = []
+            for (s, pos, box, nsteps), t_arr in zip(reqs, arrivals):
+                delay = t_arr - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(s, box, pos, nsteps))
+            for t in tickets:
+                srv.wait(t, timeout=600)
+            sts = [srv.status(t) for t in tickets]
+            for t in tickets:
+                srv.result(t)
+        lat = np.array([st.done_s - st.submit_s for st in sts])
+        span = max(st.done_s for st in sts) - min(st.submit_s for st in sts)
+        q = lambda x, p: float(np.percentile(x, p))
+        results.append({"rate_per_s": lam, "requests": len(reqs),
+                        "served": {"scenes_per_s": len(reqs) / span, "p50_s": q(lat, 50),
+                                   "p95_s": q(lat, 95), "p99_s": q(lat, 99)},
+                        "sequential": {"scenes_per_s": len(reqs) / span_seq, "p50_s": q(lat_seq, 50),
+                                       "p95_s": q(lat_seq, 95), "p99_s": q(lat_seq, 99)}})
+    line = {"metric": "served scenes/s and completion latency", "unit": "scenes/s",
+            "value": results[-1]["served"]["scenes_per_s"], "higher_is_better": True, "n_gpus": 1,
+            "dtype": "f32", "data": "synthetic (seeded Poisson stream)",
+            "config": {"workload": "requests: N log-uniform [2000, 500000], steps U[100, 2000], "
+                                   "k U[10,40], mu U[0.5,3]; HBM budget 150 GB",
+                       "steps_per_tick": a.tick},
+            "rates": results}
+    print(json.dumps(line), flush=True)
 
 
 def run_reference(a):
@@ -207,13 +357,8 @@ def run_sphx(a):
         sc.synchronize()
         torch.cuda.synchronize(device)
     barrier()
-    ms = e0.elapsed_time(e1)
+    ms = max_over_ranks(e0.elapsed_time(e1))
     kt = sc.kernel_times()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     value = n * a.steps * world / (ms / 1e3)
 
     peak, peak_kind = peaks()
@@ -248,29 +393,50 @@ def run_sphx(a):
                                                None, None, None))
     t_e2e = time.perf_counter() - t0
     barrier()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_e2e], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(t_e2e)
     e2e = {"value": n * e2e_steps * world / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
            "path": "sphx_set_state + sphx_step + sphx_read_state (pinned host buffers)"}
     sc.close()
 
+    # The configured run (200 steps from the initial lattice, graph replay):
+    # the fluid clumps as it falls (the reference's physics at these
+    # constants), so later steps cost more than the timed window above.
+    config_run = None
+    if a.config_steps > 0:
+        sc = sphx.Scene(s, box, pos, None, sphx.default_options(device=device, use_graph=1))
+        stream = torch.cuda.ExternalStream(sc.device_view().stream, device=device)
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        sc.step(sphx.DT, a.config_steps)
+        c1.record(stream)
+        sc.synchronize()
+        cms = max_over_ranks(c0.elapsed_time(c1))
+        sc.close()
+        config_run = {"steps": a.config_steps, "ms_per_step": cms / a.config_steps,
+                      "particle_steps_per_s": n * a.config_steps * world / (cms / 1e3),
+                      "note": "whole configured run from the initial lattice, CUDA graph replay"}
+
     if rank != 0:
         return
     cpu = cpu_baseline(pos, box, s) if world == 1 and not a.no_cpu else None
+    batched = None
+    if world == 1 and a.batch_steps > 0:
+        import sphx
+        batched = batch_compare(sphx.batch_scenes(512, seed=0), a.batch_steps, 0, device)
     ws_mb = n * (16 * 4 + 4 * 2 + 8 + 16 + 12) / 1e6
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded SplitMix64 jittered lattice)",
             "config": {"workload": WORKLOAD, "reorder_interval": a.reorder,
+                       "timed_window": "steps %d..%d of the run from the initial lattice" % (a.warmup, a.warmup + a.steps),
                        "l2": "inputs larger than L2: per-step working set %.0f MB > 129 MB, no flush" % ws_mb,
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-            "clocks": clk.summary(), "gpu_launches": int(kt.launches)}
+            "clocks": clk.summary(), "gpu_launches": int(kt.launches), "batched": batched,
+            "config_run": config_run}
     print(json.dumps(line), flush=True)
 
 
@@ -280,6 +446,14 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="sphx", choices=["sphx", "reference"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve"])
+    ap.add_argument("--batch-steps", type=int, default=20,
+                    help="steps of the batched-vs-sequential comparison in the plain run (0: skip)")
+    ap.add_argument("--requests", type=int, default=32)
+    ap.add_argument("--config-steps", type=int, default=200,
+                    help="steps of the whole-configuration run reported as config_run (0: skip)")
+    ap.add_argument("--rates", default="50,100,200,500,1000,2000")
+    ap.add_argument("--tick", type=int, default=10)
     ap.add_argument("--reorder", type=int, default=1)
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per density+force step, if captured")
@@ -289,6 +463,10 @@ def main():
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "batch":
+        run_batch(a)
+    elif a.workload == "serve":
+        run_serve(a)
     else:
         run_sphx(a)
 

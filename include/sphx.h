@@ -64,8 +64,28 @@ typedef struct sphx_options {
     float grid_ymax;       /* top of the cell grid without a ceiling; <= ymin: automatic */
     int grid_dims[3];      /* cell-grid dimensions; 0: automatic (each >= 5) */
     int grid_origin[3];    /* cell coordinates of grid slot 0 (used when grid_dims set) */
-    uint32_t max_cell_occupancy; /* particles per cell before a step fails (0: 1024) */
+    uint32_t max_cell_occupancy; /* particles per cell before a step fails (0 or > 16384: 16384) */
+    int density_threads;   /* block size of the density kernel: 128 or 256 (0: 256) */
+    int force_threads;     /* block size of the force kernel: 128 or 256 (0: 256) */
 } sphx_options;
+
+/* One scene of a batch: its settings, walls and initial host state. */
+typedef struct sphx_scene_desc {
+    sphx_settings settings;
+    sphx_box box;
+    size_t n;
+    const float *pos3;
+    const float *vel3; /* NULL: zero */
+} sphx_scene_desc;
+
+/* Launch configuration of the step kernels; ms_per_step is what the
+ * autotuner measured for it (0 if not measured). */
+typedef struct sphx_tuning {
+    int density_threads;
+    int force_threads;
+    int reorder_interval;
+    double ms_per_step;
+} sphx_tuning;
 
 /* Dam-break lattice block: index i + nx*(j + ny*k), position
  * origin + (i, j, k) * spacing + jitter, jitter uniform in [-amp, amp) per
@@ -134,8 +154,34 @@ int sphx_reference_scene(size_t cube_width, float h, float *pos3);
  * box NULL: the reference box; opt NULL: sphx_options_default. */
 int sphx_create(const sphx_settings *s, const sphx_box *box, const sphx_options *opt, size_t n,
                 const float *pos3, const float *vel3, sphx_handle **out);
+/* Batched form (no counterpart in the reference, which simulates one scene):
+ * nscenes independent scenes of uneven sizes and settings, resident in one
+ * handle and advanced together, each kernel launch covering every scene.
+ * All handle functions apply; arrays are the scenes concatenated in order,
+ * each in its own id order (sphx_scene_range gives a scene's rows). */
+int sphx_create_batch(const sphx_scene_desc *scenes, size_t nscenes, const sphx_options *opt,
+                      sphx_handle **out);
+/* A scene whose dam-break lattice (sphx_lattice_desc) is generated on the
+ * device, bit-identical to sphx_lattice: no host positions, no upload. */
+int sphx_create_lattice(const sphx_settings *s, const sphx_box *box, const sphx_options *opt,
+                        const sphx_lattice_desc *lattice, sphx_handle **out);
+/* Replaces scene `scene` of a handle with a new one (desc->settings, box and
+ * either host state or, when lattice is not NULL, a device-generated
+ * lattice), as the reference GUI's RESET re-creates its system
+ * (Tester.cpp:148-173); the other scenes keep their state.  The arena is
+ * reused while the new layout fits it. */
+int sphx_replace_scene(sphx_handle *h, size_t scene, const sphx_scene_desc *desc,
+                       const sphx_lattice_desc *lattice);
+/* Changes a scene's settings (and walls, if box is not NULL) keeping its
+ * particles; the cell grid is re-sized when h or the box changes. */
+int sphx_set_settings(sphx_handle *h, size_t scene, const sphx_settings *s, const sphx_box *box);
 int sphx_destroy(sphx_handle *h);
 size_t sphx_count(const sphx_handle *h);
+size_t sphx_scene_count(const sphx_handle *h);
+int sphx_scene_range(const sphx_handle *h, size_t scene, size_t *first, size_t *count);
+/* One scene's state, host, scene-local id order; any pointer may be NULL. */
+int sphx_read_scene(sphx_handle *h, size_t scene, float *pos3, float *vel3, float *rho,
+                    float *prs, float *force3);
 /* Replaces positions / velocities (host, id order, vel3 may be NULL) and
  * clears an error state. */
 int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3);
@@ -187,9 +233,79 @@ int sphx_update_particles_release(void);
 int sphx_density_static(const sphx_settings *s, const void *d_pos4, size_t n, float *d_rho,
                         float *d_prs, void *stream);
 
+int sphx_get_tuning(const sphx_handle *h, sphx_tuning *out);
+int sphx_set_tuning(sphx_handle *h, const sphx_tuning *t);
+/* Times every candidate configuration (density / force block size 128 or
+ * 256, reorder interval 1, 2 or 4) over trial_steps steps of dt on this
+ * handle's scenes, applies the fastest and returns it.  The handle's state
+ * is restored afterwards.  With cache_path set, a configuration recorded
+ * there for the same device and workload signature (particle count, scene
+ * count) is applied without timing, and new results are appended. */
+int sphx_autotune(sphx_handle *h, float dt, int trial_steps, const char *cache_path,
+                  sphx_tuning *out);
+
 int sphx_set_profiling(sphx_handle *h, int enable);
 /* Synchronises, then returns the accumulated per-phase times and resets them. */
 int sphx_get_kernel_times(sphx_handle *h, sphx_kernel_times *out);
+
+/* ---- Served form (no counterpart in the reference): a continuous-batching
+ * request loop.  Each request is a scene plus a step count; a worker thread
+ * admits queued requests in arrival order while their device footprint fits
+ * the HBM budget, advances every admitted scene together in one batch,
+ * retires each scene when it reaches its step count and admits the next
+ * ones as memory frees up.  A result equals that of the same scene run
+ * alone with the same dt. */
+#define SPHX_REQ_QUEUED 0
+#define SPHX_REQ_RUNNING 1
+#define SPHX_REQ_DONE 2
+#define SPHX_REQ_FAILED 3
+
+typedef struct sphx_server sphx_server;
+
+typedef struct sphx_server_options {
+    size_t hbm_budget_bytes; /* admission budget (default 150 GB) */
+    int steps_per_tick;      /* steps between admission/retirement points (default 10) */
+    int max_scenes;          /* resident scene limit, 0: none */
+    float dt;                /* step size of every request (default 0.002) */
+    int device;
+} sphx_server_options;
+
+typedef struct sphx_request {
+    sphx_settings settings;
+    sphx_box box;
+    size_t n;
+    const float *pos3; /* host, copied at submission */
+    const float *vel3; /* NULL: zero */
+    int nsteps;
+} sphx_request;
+
+typedef struct sphx_request_status {
+    int state;       /* SPHX_REQ_* */
+    int steps_done;
+    double submit_s; /* seconds since the server started */
+    double admit_s;
+    double done_s;
+} sphx_request_status;
+
+typedef struct sphx_server_stats {
+    uint64_t submitted, completed, ticks, relayouts, particle_steps;
+    size_t live_scenes, queued, bytes_in_use;
+    double elapsed_s;
+} sphx_server_stats;
+
+void sphx_server_options_default(sphx_server_options *o);
+int sphx_server_create(const sphx_server_options *opt, sphx_server **out);
+int sphx_server_submit(sphx_server *s, const sphx_request *r, uint64_t *ticket);
+int sphx_server_status(sphx_server *s, uint64_t ticket, sphx_request_status *out);
+/* Blocks until the request is done (SPHX_OK), failed, or timeout_s passes
+ * (SPHX_ERR_STATE). */
+int sphx_server_wait(sphx_server *s, uint64_t ticket, double timeout_s);
+/* Copies a finished request's final state (id order; any pointer may be
+ * NULL) and releases it. */
+int sphx_server_result(sphx_server *s, uint64_t ticket, float *pos3, float *vel3, float *rho,
+                       float *prs);
+int sphx_server_stats_get(sphx_server *s, sphx_server_stats *out);
+int sphx_server_destroy(sphx_server *s);
 
 #ifdef __cplusplus
 }

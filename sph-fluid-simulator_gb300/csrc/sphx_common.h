@@ -158,8 +158,22 @@ struct StepParams {
     float ylo, yhi, xlo, xhi, zlo, zhi, damping, offset;
     int hasCeiling;
     float dt;
+    float h2w;  // h^2 (1 + 2^-18): squared half-width bound of the walk's row windows
     Grid grid;
     uint32_t n;
+};
+
+// Device-side description of the scenes one launch covers: scene s owns
+// particles [pofs[s], pofs[s+1]) and cell-grid slots [sofs[s], sofs[s+1]) of
+// the concatenated buffers, with constants params[s].  A single scene is a
+// table of one.  Particles stay inside their scene's range through every
+// sort, because the scenes' slot ranges are disjoint and ordered.
+struct SceneTable {
+    const StepParams *params;
+    const uint32_t *pofs;
+    const uint32_t *sofs;
+    uint32_t nscenes;
+    uint32_t n;  // total particles
 };
 
 }  // namespace sphx

@@ -91,13 +91,13 @@ int sphx_update_particles(void *particles, float *transforms16, size_t n,
     SPHX_CUDA(cudaSetDevice(h->opt.device));
     cudaStream_t st = h->stream;
     SPHX_CUDA(cudaMemcpyAsync(c.d_rec, particles, kRec * n, cudaMemcpyHostToDevice, st));
-    SPHX_CUDA(sphx::launch_aos_unpack((uint32_t)n, h->d.h, c.d_rec, h->pos[h->pv], h->vel[h->pv],
+    SPHX_CUDA(sphx::launch_aos_unpack((uint32_t)n, h->scenes[0].d.h, c.d_rec, h->pos[h->pv], h->vel[h->pv],
                                       h->id[h->idc], c.d_hash, st));
     SPHX_CUDA(cudaMemsetAsync(h->sb.status, 0, 8, st));
     h->error = 0;
     int rc = sphx::run_steps(h, dt, 1);
     if (rc) return rc;
-    SPHX_CUDA(sphx::launch_aos_pack((uint32_t)n, h->d.h / 2.f, c.d_rec, h->id[h->idc],
+    SPHX_CUDA(sphx::launch_aos_pack((uint32_t)n, h->scenes[0].d.h / 2.f, c.d_rec, h->id[h->idc],
                                     h->pos[h->pv], h->vel[h->pv], h->force, h->rp, c.d_hash,
                                     transforms16 ? c.d_tr : nullptr, st));
     SPHX_CUDA(cudaMemcpyAsync(particles, c.d_rec, kRec * n, cudaMemcpyDeviceToHost, st));

@@ -25,13 +25,11 @@
 #include "sphx_common.h"
 #include "sphx_kernels.h"
 
-// Minimum resident CTAs of 256 threads per SM for the two walk kernels
-// (caps their registers at 65536 / (256 * N)).
-#ifndef SPHX_DENSITY_MIN_BLOCKS
-#define SPHX_DENSITY_MIN_BLOCKS 4
-#endif
-#ifndef SPHX_FORCE_MIN_BLOCKS
-#define SPHX_FORCE_MIN_BLOCKS 4
+// Resident threads per SM the two walk kernels are compiled for (register
+// cap 65536 / SPHX_WALK_THREADS_PER_SM); the block size is a template
+// parameter chosen per launch (128 or 256, see Tuning).
+#ifndef SPHX_WALK_THREADS_PER_SM
+#define SPHX_WALK_THREADS_PER_SM 1024
 #endif
 
 namespace sphx {
@@ -63,18 +61,32 @@ __device__ __forceinline__ CellPos cell_pos(float4 p, float h) {
 
 __device__ __forceinline__ bool in_domain(float q) { return fabsf(q) < 1073741824.0f; }
 
+// Scene of particle (storage index) i: the last s with pofs[s] <= i.
+__device__ __forceinline__ uint32_t scene_of(const SceneTable &T, uint32_t i) {
+    if (T.nscenes == 1) return 0;
+    uint32_t lo = 0, hi = T.nscenes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (T.pofs[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 // ---------------------------------------------------------------- keys / sort
 
-__global__ void k_keys(StepParams P, const float4 *__restrict__ pos, uint32_t *__restrict__ key,
+__global__ void k_keys(SceneTable T, const float4 *__restrict__ pos, uint32_t *__restrict__ key,
                        uint32_t *__restrict__ rank, uint32_t *__restrict__ count,
                        uint32_t *__restrict__ status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.n) return;
+    if (i >= T.n) return;
+    const uint32_t sc = scene_of(T, i);
+    const StepParams &P = T.params[sc];
     const CellPos c = cell_pos(pos[i], P.h);
-    uint32_t k = 0;
+    uint32_t k = T.sofs[sc];
     if (in_domain(c.qx) && in_domain(c.qy) && in_domain(c.qz)) {
         int mx, my, mz;
-        k = slot_of(P.grid, c.cx, c.cy, c.cz, mx, my, mz);
+        k += slot_of(P.grid, c.cx, c.cy, c.cz, mx, my, mz);
         // a cell outside the grid's x extent shares its slot with a cell gx
         // away: rows are then no longer sorted by x across their cells
         if ((unsigned)(c.cx - P.grid.ox) >= (unsigned)P.grid.gx) status[1] = 1u;
@@ -199,14 +211,24 @@ __global__ void k_scatter(uint32_t n, const uint32_t *__restrict__ key,
 // The particle that arrived first in a cell sorts the cell's run by
 // (x, particle index): deterministic, and it makes every run of
 // x-consecutive cells sorted by x, which the walk's x window relies on.
+// Runs longer than kSmallCell (clumped fluid) are queued for
+// k_cellsort_large instead.
+constexpr uint32_t kSmallCell = 64;
+
 __global__ void k_cellsort(uint32_t n, const float4 *__restrict__ pos,
                            const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
                            const uint32_t *__restrict__ start, uint32_t *__restrict__ order,
-                           const uint32_t *__restrict__ status) {
+                           uint32_t *__restrict__ status, uint2 *__restrict__ large,
+                           uint32_t large_cap) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || rank[i] != 0u || (*status & kStatusOverflowBit)) return;
+    if (i >= n || rank[i] != 0u || (status[0] & kStatusOverflowBit)) return;
     const uint32_t k = key[i];
     const uint32_t a = start[k], b = start[k + 1];
+    if (b - a > kSmallCell) {
+        const uint32_t slot = atomicAdd(&status[2], 1u);
+        if (slot < large_cap) large[slot] = make_uint2(a, b - a);
+        return;
+    }
     for (uint32_t x = a + 1; x < b; ++x) {
         const uint32_t v = order[x];
         const float vx = pos[v].x;
@@ -219,6 +241,56 @@ __global__ void k_cellsort(uint32_t n, const float4 *__restrict__ pos,
             --y;
         }
         order[y] = v;
+    }
+}
+
+// Total order of floats as unsigned integers (finite values).
+__device__ __forceinline__ uint32_t float_order(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// One CTA per queued large cell: bitonic sort of (x, particle index) keys in
+// shared memory (up to kLargeCell entries), written back to the cell's run.
+__global__ void __launch_bounds__(512) k_cellsort_large(const float4 *__restrict__ pos,
+                                                        uint32_t *__restrict__ order,
+                                                        const uint32_t *__restrict__ status,
+                                                        const uint2 *__restrict__ large,
+                                                        uint32_t large_cap) {
+    extern __shared__ unsigned long long skeys[];
+    if (status[0] & kStatusOverflowBit) return;
+    const uint32_t count = min(status[2], large_cap);
+    for (uint32_t c = blockIdx.x; c < count; c += gridDim.x) {
+        const uint2 cell = large[c];  // (start, length), length <= kLargeCell
+        uint32_t m = 2;
+        while (m < cell.y) m <<= 1;
+        for (uint32_t t = threadIdx.x; t < m; t += blockDim.x) {
+            unsigned long long v = ~0ull;
+            if (t < cell.y) {
+                const uint32_t j = order[cell.x + t];
+                v = ((unsigned long long)float_order(pos[j].x) << 32) | j;
+            }
+            skeys[t] = v;
+        }
+        __syncthreads();
+        for (uint32_t k = 2; k <= m; k <<= 1)
+            for (uint32_t jj = k >> 1; jj > 0; jj >>= 1) {
+                for (uint32_t t = threadIdx.x; t < m; t += blockDim.x) {
+                    const uint32_t u = t ^ jj;
+                    if (u > t) {
+                        const unsigned long long x = skeys[t], y = skeys[u];
+                        const bool up = (t & k) == 0;
+                        if ((x > y) == up) {
+                            skeys[t] = y;
+                            skeys[u] = x;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        for (uint32_t t = threadIdx.x; t < cell.y; t += blockDim.x)
+            order[cell.x + t] = (uint32_t)skeys[t];
+        __syncthreads();
     }
 }
 
@@ -240,10 +312,11 @@ __global__ void k_gather(uint32_t n, const uint32_t *__restrict__ order,
 struct WalkCtx {
     const float4 *__restrict__ pos;
     const uint32_t *__restrict__ order;
-    const uint32_t *__restrict__ start;
+    const uint32_t *__restrict__ start;  // this scene's first slot
     Grid grid;
     float h2;
-    float hx;  // x half-width of the row window: h (1 + 2^-20)
+    float h;
+    float h2w;  // h^2 (1 + 2^-18): squared half-width bound of the row windows
     bool xmono;  // every particle inside the grid's x extent this step
 };
 
@@ -320,28 +393,68 @@ __device__ __forceinline__ uint32_t row_base(const Grid &g, int my, int mz, int 
     return ((uint32_t)z * (uint32_t)g.gy + (uint32_t)y) * (uint32_t)g.gx;
 }
 
+// Lower bound on the distance from coordinate y (quotient cell c) to any
+// particle of cell c + d, d = +1 or -1.  Cell m covers quotients [m, m+1) for
+// m > 0, (m-1, m] for m < 0 and (-1, 1) for m = 0.  A particle can sit in
+// cell m while a few ulps past m*h (the division rounds), so the bound is
+// lowered by (|y| + |bound| + h) 2^-20 and clamped at 0.
+__device__ __forceinline__ float gap_to_cell(float y, int c, int d, float h) {
+    float bound, gap;
+    if (d > 0) {
+        const int m = c + 1;
+        bound = (float)(m > 0 ? m : m - 1) * h;
+        gap = bound - y;
+    } else {
+        const int m = c - 1;
+        bound = (float)(m >= 0 ? m + 1 : m) * h;
+        gap = y - bound;
+    }
+    const float slack = (fabsf(y) + fabsf(bound) + h) * 9.5367431640625e-07f;
+    return fmaxf(gap - slack, 0.f);
+}
+
 // Fast path: the 27 cells around (mx, my, mz), each visited once.  With the
 // particle's slot away from the grid's x seam, each (dy, dz) row of three
-// cells is one contiguous run; the bounds of row r+1 are loaded before row r
-// is scanned.
+// cells is one contiguous, x-sorted run.  A row whose cells are at least
+// (ey, ez) away in y and z can only hold accepted particles with
+// dx^2 < h^2 - ey^2 - ez^2, so it is scanned inside that narrower x window
+// and skipped when the window is empty; the bounds of the next row to scan
+// are loaded before the current one is scanned.
 template <bool kInd, class V>
-__device__ __forceinline__ void walk_rows(const WalkCtx &W, int mx, int my, int mz, uint32_t self,
-                                          float4 pi, V &vis) {
+__device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, int mx, int my,
+                                          int mz, uint32_t self, float4 pi, V &vis) {
     const Grid &g = W.grid;
     if (mx >= 1 && mx + 1 < g.gx) {
-        const float hx = fmaf(fabsf(pi.x), 2.384185791015625e-07f, W.hx);  // + |x| 2^-22
-        const float xlo = pi.x - hx, xhi = pi.x + hx;
-        uint32_t base = row_base(g, my, mz, 0);
+        const float h = W.h;
+        const float eym = gap_to_cell(pi.y, c.cy, -1, h), eyp = gap_to_cell(pi.y, c.cy, 1, h);
+        const float ezm = gap_to_cell(pi.z, c.cz, -1, h), ezp = gap_to_cell(pi.z, c.cz, 1, h);
+        const float ey2[3] = {eym * eym, 0.f, eyp * eyp};
+        const float ez2[3] = {ezm * ezm, 0.f, ezp * ezp};
+        uint32_t rows = 0;
+#pragma unroll
+        for (int r = 0; r < 9; ++r)
+            if (W.h2w - ey2[r % 3] - ez2[r / 3] > 0.f) rows |= 1u << r;
+        const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
+        int r = __ffs(rows) - 1;
+        rows &= rows - 1;
+        uint32_t base = row_base(g, my, mz, r);
         uint32_t a = W.start[base + mx - 1], b = W.start[base + mx + 2];
 #pragma unroll 1
-        for (int r = 0; r < 9; ++r) {
+        while (r >= 0) {
             const uint32_t ca = a, cb = b;
-            if (r < 8) {
-                base = row_base(g, my, mz, r + 1);
+            const int cr = r;
+            r = rows ? __ffs(rows) - 1 : -1;
+            rows &= rows - 1;
+            if (r >= 0) {
+                base = row_base(g, my, mz, r);
                 a = W.start[base + mx - 1];
                 b = W.start[base + mx + 2];
             }
-            scan_run_x<kInd>(W, ca, cb, self, pi, xlo, xhi, W.xmono, vis);
+            const int iy = cr % 3, iz = cr / 3;
+            const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
+            const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
+            const float hx = fmaf(sqrtf(W.h2w - eyy - ezz), 1.0000009536743164f, xpad);
+            scan_run_x<kInd>(W, ca, cb, self, pi, pi.x - hx, pi.x + hx, W.xmono, vis);
         }
     } else {
 #pragma unroll 1
@@ -423,7 +536,7 @@ template <bool kInd, class V>
 __device__ __forceinline__ void walk(const WalkCtx &W, const WalkStart &s, uint32_t self, float4 pi,
                                      V &vis) {
     if (s.flags == 0u)
-        walk_rows<kInd>(W, s.mx, s.my, s.mz, self, pi, vis);
+        walk_rows<kInd>(W, s.c, s.mx, s.my, s.mz, self, pi, vis);
     else
         walk_slow<kInd>(W, s.c.cx, s.c.cy, s.c.cz, s.flags, self, pi, vis);
 }
@@ -440,33 +553,68 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
     s = t;
 }
 
+// Accepted neighbours of a particle, in walk order, are also recorded for
+// the force kernel: list row k of particle i is nbr[k * stride + i], k <
+// kNbrSlots; a particle with more (clumped fluid) stores its count only and
+// the force kernel walks for it instead.
+constexpr uint32_t kNbrSlots = 64;
+
 struct DensityVisitor {
     float h2;
     float acc, comp;  // compensated sum of (h^2 - r^2)^3
-    __device__ __forceinline__ void operator()(uint32_t, float, float, float, float d2) {
+    uint32_t *row;    // &nbr[i]
+    uint32_t stride;
+    uint32_t cnt;
+    __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float d2) {
         const float u = __fsub_rn(h2, d2);
         kahan_add(acc, comp, __fmul_rn(__fmul_rn(u, u), u));
+        if (row && cnt < kNbrSlots) row[cnt * stride] = j;
+        ++cnt;
     }
 };
 
 // sph.cpp:28-76.  The reference accumulates m*poly6*(h^2-r^2)^3 term by term;
 // here the cubes are summed and scaled once (the two differ by float
 // rounding only).
-template <bool kInd>
-__global__ void __launch_bounds__(256, SPHX_DENSITY_MIN_BLOCKS) k_density(StepParams P, WalkCtx W, float4 *__restrict__ rp,
-                                                 const uint32_t *__restrict__ status) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n || (status[0] & kStatusErrorMask)) return;
+// Per-thread walk context of scene sc.
+__device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &G, uint32_t sc,
+                                            const StepParams &P, const uint32_t *status) {
+    WalkCtx W = G;
+    W.start = G.start + T.sofs[sc];
+    W.grid = P.grid;
+    W.h2 = P.h2;
+    W.h = P.h;
+    W.h2w = P.h2w;
     W.xmono = status[1] == 0u;
-    const uint32_t i = kInd ? W.order[t] : t;
+    return W;
+}
+
+template <bool kInd, int kThreads>
+__global__ void __launch_bounds__(kThreads, SPHX_WALK_THREADS_PER_SM / kThreads)
+    k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
+              float4 *__restrict__ fr, NbrList L, const uint32_t *__restrict__ status) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= T.n || (status[0] & kStatusErrorMask)) return;
+    const uint32_t i = kInd ? G.order[t] : t;
+    const uint32_t sc = scene_of(T, i);
+    const StepParams &P = T.params[sc];
+    const WalkCtx W = walk_ctx(T, G, sc, P, status);
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
-    DensityVisitor v{P.h2, 0.f, 0.f};
+    DensityVisitor v{P.h2, 0.f, 0.f, L.nbr ? L.nbr + i : nullptr, L.stride, 0u};
     walk<kInd>(W, s, i, pi, v);
     const float rho = __fadd_rn(__fmul_rn(P.mp6, v.acc), P.selfDens);
     const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
-    rp[i] = make_float4(rho, prs, __frcp_rn(rho), 0.f);
+    const float inv = __frcp_rn(rho);
+    rp[i] = make_float4(rho, prs, inv, 0.f);
+    if (L.nbr) {
+        L.count[i] = v.cnt;
+        // what the force kernel reads of a neighbour, in one 32-byte record
+        const float4 vi = vel[i];
+        fr[2 * (size_t)i] = make_float4(pi.x, pi.y, pi.z, prs);
+        fr[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, inv);
+    }
 }
 
 // One accepted pair of sph.cpp:107-121.  With d = pj - pi, r = |d| and
@@ -479,55 +627,56 @@ __global__ void __launch_bounds__(256, SPHX_DENSITY_MIN_BLOCKS) k_density(StepPa
 // Per term this moves the result by a few float ulps; summed forces stay
 // within about 1e-6 of the reference's (rms-floored relative metric).
 struct ForcePair {
-    const float4 *__restrict__ vel;
-    const float4 *__restrict__ rp;
     float4 vi;
     float presI, h, kp, kv;
     float fx, fy, fz;
     float cx, cy, cz;  // Kahan compensations
-    __device__ __forceinline__ void operator()(uint32_t j, float dx, float dy, float dz, float d2) {
-        const float4 vj = vel[j];
-        const float4 q = rp[j];
+    // pj_w = neighbour pressure, vj = (velocity, 1/density)
+    __device__ __forceinline__ void add(float dx, float dy, float dz, float d2, float pj_w,
+                                        float4 vj) {
         const float invr = rsqrtf(d2);
         const float r = d2 * invr;
         const float hd = h - r;
-        const float cp = kp * (presI + q.y) * q.z * (hd * hd) * invr;
-        const float cv = kv * hd * q.z;
+        const float cp = kp * (presI + pj_w) * vj.w * (hd * hd) * invr;
+        const float cv = kv * hd * vj.w;
         kahan_add(fx, cx, fmaf(cv, vj.x - vi.x, -cp * dx));
         kahan_add(fy, cy, fmaf(cv, vj.y - vi.y, -cp * dy));
         kahan_add(fz, cz, fmaf(cv, vj.z - vi.z, -cp * dz));
     }
 };
 
+// r^2 of the reference (sph.cpp:57) from a neighbour's record, then the pair.
+__device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *__restrict__ fr,
+                                                 uint32_t j, float4 pi) {
+    const float4 a = fr[2 * (size_t)j];
+    const float4 b = fr[2 * (size_t)j + 1];
+    const float dx = __fsub_rn(a.x, pi.x);
+    const float dy = __fsub_rn(a.y, pi.y);
+    const float dz = __fsub_rn(a.z, pi.z);
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    pair.add(dx, dy, dz, d2, a.w, b);
+}
+
 // The force walk in two phases: the candidate test only appends accepted
 // neighbours to this thread's column of a shared-memory list; the pair
 // math then runs over the list with every lane busy, instead of under the
 // acceptance branch (about 1 candidate in 4 passes) with most lanes idle.
-constexpr int kForceThreads = 256;
 constexpr int kForceList = 48;  // list slots per thread (flushed when full)
 
+template <int kThreads>
 struct ForceListVisitor {
-    uint32_t *list;  // this thread's column: list[k * kForceThreads]
+    uint32_t *list;  // this thread's column: list[k * kThreads]
     uint32_t cnt;
-    const float4 *__restrict__ pos;
+    const float4 *__restrict__ fr;
     float4 pi;
     ForcePair pair;
     __device__ __forceinline__ void flush() {
 #pragma unroll 1
-        for (uint32_t k = 0; k < cnt; ++k) {
-            const uint32_t j = list[k * kForceThreads];
-            const float4 pj = pos[j];
-            const float dx = __fsub_rn(pj.x, pi.x);
-            const float dy = __fsub_rn(pj.y, pi.y);
-            const float dz = __fsub_rn(pj.z, pi.z);
-            const float d2 =
-                __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            pair(j, dx, dy, dz, d2);
-        }
+        for (uint32_t k = 0; k < cnt; ++k) pair_from_record(pair, fr, list[k * kThreads], pi);
         cnt = 0;
     }
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float) {
-        list[cnt * kForceThreads] = j;
+        list[cnt * kThreads] = j;
         if (++cnt == (uint32_t)kForceList) flush();
     }
 };
@@ -572,27 +721,37 @@ __device__ __forceinline__ void integrate(const StepParams &P, float4 &x, float4
     }
 }
 
-template <bool kInd>
-__global__ void __launch_bounds__(kForceThreads, SPHX_FORCE_MIN_BLOCKS)
-    k_force(StepParams P, WalkCtx W, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
-            float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
-            float4 *__restrict__ force_out, const uint32_t *__restrict__ status) {
-    __shared__ uint32_t s_list[kForceList * kForceThreads];
+template <bool kInd, int kThreads>
+__global__ void __launch_bounds__(kThreads, SPHX_WALK_THREADS_PER_SM / kThreads)
+    k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
+            const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
+            float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
+            const uint32_t *__restrict__ status) {
+    __shared__ uint32_t s_list[kForceList * kThreads];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n || (status[0] & kStatusErrorMask)) return;
-    W.xmono = status[1] == 0u;
-    const uint32_t i = kInd ? W.order[t] : t;
+    if (t >= T.n || (status[0] & kStatusErrorMask)) return;
+    const uint32_t i = kInd ? G.order[t] : t;
+    const uint32_t sc = scene_of(T, i);
+    const StepParams &P = T.params[sc];
+    const WalkCtx W = walk_ctx(T, G, sc, P, status);
     float4 pi = W.pos[i];
     float4 vi = vel[i];
     const float4 q = rp[i];
-    WalkStart s;
-    walk_start(P, pi, s);
-    ForceListVisitor v{s_list + threadIdx.x, 0u, W.pos, pi,
-                       ForcePair{vel, rp, vi, q.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f,
-                                 0.f, 0.f}};
-    walk<kInd>(W, s, i, pi, v);
-    v.flush();
-    const float fx = v.pair.fx, fy = v.pair.fy, fz = v.pair.fz;
+    ForcePair pair{vi, q.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const uint32_t cnt = L.count[i];
+    if (cnt <= kNbrSlots) {  // the density kernel's list, same neighbours, same order
+        const uint32_t *row = L.nbr + i;
+#pragma unroll 1
+        for (uint32_t k = 0; k < cnt; ++k) pair_from_record(pair, fr, row[(size_t)k * L.stride], pi);
+    } else {
+        WalkStart s;
+        walk_start(P, pi, s);
+        ForceListVisitor<kThreads> v{s_list + threadIdx.x, 0u, fr, pi, pair};
+        walk<kInd>(W, s, i, pi, v);
+        v.flush();
+        pair = v.pair;
+    }
+    const float fx = pair.fx, fy = pair.fy, fz = pair.fz;
     force_out[i] = make_float4(fx, fy, fz, 0.f);
     integrate(P, pi, vi, fx, fy, fz, q.x);
     pos_out[i] = pi;
@@ -619,41 +778,95 @@ struct DigestVisitor {
 };
 
 template <bool kInd>
-__global__ void k_digest(StepParams P, WalkCtx W, const uint32_t *__restrict__ id,
+__global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ id,
                          uint32_t *__restrict__ count_out, uint64_t *__restrict__ digest_out,
                          const uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= P.n || (status[0] & kStatusErrorMask)) return;
-    W.xmono = status[1] == 0u;
-    const uint32_t i = kInd ? W.order[t] : t;
+    if (t >= T.n || (status[0] & kStatusErrorMask)) return;
+    const uint32_t i = kInd ? G.order[t] : t;
+    const uint32_t sc = scene_of(T, i);
+    const StepParams &P = T.params[sc];
+    const WalkCtx W = walk_ctx(T, G, sc, P, status);
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
     DigestVisitor v{id, 0u, 0ull};
     walk<kInd>(W, s, i, pi, v);
-    count_out[id[i]] = v.count;
-    digest_out[id[i]] = v.sum;
+    const uint32_t d = T.pofs[sc] + id[i];
+    count_out[d] = v.count;
+    digest_out[d] = v.sum;
 }
 
-__global__ void k_upload(uint32_t n, const float *__restrict__ pos3, const float *__restrict__ vel3,
-                         float4 *__restrict__ pos, float4 *__restrict__ vel,
-                         uint32_t *__restrict__ id) {
+// Rows [first, first + n) from host-ordered staging arrays (vel3 all zero
+// or uploaded); ids are scene-local: row - first.
+__global__ void k_upload_rows(uint32_t first, uint32_t n, const float *__restrict__ pos3,
+                              const float *__restrict__ vel3, float4 *__restrict__ pos,
+                              float4 *__restrict__ vel, uint32_t *__restrict__ id) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    pos[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], 0.f);
-    vel[i] = vel3 ? make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.f)
-                  : make_float4(0.f, 0.f, 0.f, 0.f);
-    id[i] = i;
+    const uint32_t r = first + i;
+    pos[r] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], 0.f);
+    vel[r] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.f);
+    id[r] = i;
+}
+
+// The dam-break lattice of sphx_lattice (host, sphx_host.cpp) generated in
+// place: same SplitMix64 counters and the same float operations in the same
+// order, so rows are bit-identical to the host generator's.  Velocity 0.
+__global__ void k_lattice_rows(uint32_t first, LatticeGen L, float4 *__restrict__ pos,
+                               float4 *__restrict__ vel, uint32_t *__restrict__ id) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t n = L.nx * L.ny * L.nz;
+    if (idx >= n) return;
+    const uint32_t k = idx / (L.nx * L.ny), rem = idx - k * L.nx * L.ny;
+    const uint32_t j = rem / L.nx, i = rem - j * L.nx;
+    const uint32_t ijk[3] = {i, j, k};
+    float out[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        uint64_t z = L.seed + (3ull * idx + (uint64_t)a) * 0x9E3779B97F4A7C15ull + 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const float u = __fmul_rn(__ull2float_rn(z >> 40), 5.9604644775390625e-08f);  // 2^-24
+        const float jit = __fmul_rn(__fsub_rn(__fmul_rn(u, 2.0f), 1.0f), L.jitter);
+        const float base = __fadd_rn(L.origin[a], __fmul_rn(__uint2float_rn(ijk[a]), L.spacing));
+        out[a] = __fadd_rn(base, jit);
+    }
+    const uint32_t r = first + idx;
+    pos[r] = make_float4(out[0], out[1], out[2], 0.f);
+    vel[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+    id[r] = idx;
+}
+
+// One scene's rows [first, first + n) to staging in scene-local id order.
+// field: 0 pos, 1 vel, 2 force, 3 rho, 4 prs.
+__global__ void k_read_rows(uint32_t first, uint32_t n, int field, const uint32_t *__restrict__ id,
+                            const float4 *__restrict__ v4, const float4 *__restrict__ rp,
+                            float *__restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t r = first + i;
+    const uint32_t d = id[r];
+    if (field <= 2) {
+        const float4 v = v4[r];
+        out[3 * d] = v.x;
+        out[3 * d + 1] = v.y;
+        out[3 * d + 2] = v.z;
+    } else {
+        const float4 q = rp[r];
+        out[d] = field == 3 ? q.x : q.y;
+    }
 }
 
 // Field readout in id order: 3 floats per particle for vec fields, 1 for
 // scalars.  field: 0 pos, 1 vel, 2 force, 3 rho, 4 prs.
-__global__ void k_read_field(uint32_t n, int field, const uint32_t *__restrict__ id,
+__global__ void k_read_field(SceneTable T, int field, const uint32_t *__restrict__ id,
                              const float4 *__restrict__ v4, const float4 *__restrict__ rp,
                              float *__restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint32_t d = id[i];
+    if (i >= T.n) return;
+    const uint32_t d = T.pofs[scene_of(T, i)] + id[i];
     if (field <= 2) {
         const float4 v = v4[i];
         out[3 * d] = v.x;
@@ -668,12 +881,14 @@ __global__ void k_read_field(uint32_t n, int field, const uint32_t *__restrict__
 // translate(position) * scale(h/2) (sph.cpp:178-179), column-major, id order.
 // GLM's product leaves exact zeros off the diagonal and adds +0 to the
 // translation (so -0 reads back as +0).
-__global__ void k_transforms(uint32_t n, float half_h, const uint32_t *__restrict__ id,
+__global__ void k_transforms(SceneTable T, const uint32_t *__restrict__ id,
                              const float4 *__restrict__ pos, float4 *__restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= T.n) return;
+    const uint32_t sc = scene_of(T, i);
+    const float half_h = T.params[sc].halfH;
     const float4 p = pos[i];
-    float4 *m = out + 4 * (size_t)id[i];
+    float4 *m = out + 4 * ((size_t)T.pofs[sc] + id[i]);
     m[0] = make_float4(half_h, 0.f, 0.f, 0.f);
     m[1] = make_float4(0.f, half_h, 0.f, 0.f);
     m[2] = make_float4(0.f, 0.f, half_h, 0.f);
@@ -681,13 +896,14 @@ __global__ void k_transforms(uint32_t n, float half_h, const uint32_t *__restric
 }
 
 // Cell (truncated quotient) and stored uint16 hash per particle, id order.
-__global__ void k_cells(uint32_t n, float h, const uint32_t *__restrict__ id,
+__global__ void k_cells(SceneTable T, const uint32_t *__restrict__ id,
                         const float4 *__restrict__ pos, int *__restrict__ cells,
                         uint16_t *__restrict__ hash) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const CellPos c = cell_pos(pos[i], h);
-    const uint32_t d = id[i];
+    if (i >= T.n) return;
+    const uint32_t sc = scene_of(T, i);
+    const CellPos c = cell_pos(pos[i], T.params[sc].h);
+    const uint32_t d = T.pofs[sc] + id[i];
     if (cells) {
         cells[3 * d] = c.cx;
         cells[3 * d + 1] = c.cy;
@@ -758,22 +974,30 @@ inline unsigned blocks(uint32_t n, unsigned bs) { return (n + bs - 1) / bs; }
 
 // ---------------------------------------------------------------- launchers
 
-cudaError_t launch_sort(const StepParams &P, const SortBuffers &B, const float4 *pos,
+cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                         cudaStream_t st) {
     const unsigned bs = 256;
-    const uint32_t n = P.n;
+    const uint32_t n = T.n;
     const uint32_t m = B.slots + 1;  // count[slots] stays 0 -> start[slots] = n
     const uint32_t ntiles = (m + kScanTile - 1) / kScanTile;
-    cudaMemsetAsync(B.status + 1, 0, 4, st);
-    if (n) k_keys<<<blocks(n, bs), bs, 0, st>>>(P, pos, B.key, B.rank, B.count, B.status);
+    cudaMemsetAsync(B.status + 1, 0, 8, st);  // x-wrap flag, large-cell count
+    if (n) k_keys<<<blocks(n, bs), bs, 0, st>>>(T, pos, B.key, B.rank, B.count, B.status);
     k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.max_cell, B.status);
     k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(B.tile_sum, ntiles);
     k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.start);
     if (n) {
         k_scatter<<<blocks(n, bs), bs, 0, st>>>(n, B.key, B.rank, B.start, B.order, B.status);
-        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.order, B.status);
+        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.order,
+                                                 B.status, B.large, B.large_cap);
+        k_cellsort_large<<<kLargeBlocks, 512, 8 * kLargeCell, st>>>(pos, B.order, B.status,
+                                                                    B.large, B.large_cap);
     }
     return cudaGetLastError();
+}
+
+cudaError_t prepare_device() {
+    return cudaFuncSetAttribute(k_cellsort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                8 * kLargeCell);
 }
 
 cudaError_t launch_gather(uint32_t n, const SortBuffers &B, const float4 *pos_in,
@@ -784,79 +1008,111 @@ cudaError_t launch_gather(uint32_t n, const SortBuffers &B, const float4 *pos_in
     return cudaGetLastError();
 }
 
-static WalkCtx make_ctx(const StepParams &P, const SortBuffers &B, const float4 *pos) {
-    WalkCtx W;
+static WalkCtx global_ctx(const SortBuffers &B, const float4 *pos) {
+    WalkCtx W{};
     W.pos = pos;
     W.order = B.order;
     W.start = B.start;
-    W.grid = P.grid;
-    W.h2 = P.h2;
-    W.hx = P.h * (1.0f + 9.5367431640625e-07f);
     W.xmono = true;
     return W;
 }
 
-cudaError_t launch_density(const StepParams &P, const SortBuffers &B, const float4 *pos,
-                           float4 *rp, bool indirect, cudaStream_t st) {
-    const WalkCtx W = make_ctx(P, B, pos);
-    if (P.n) {
-        if (indirect) k_density<true><<<blocks(P.n, 256), 256, 0, st>>>(P, W, rp, B.status);
-        else k_density<false><<<blocks(P.n, 256), 256, 0, st>>>(P, W, rp, B.status);
+template <int kThreads>
+static void density_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel, float4 *rp,
+                           float4 *fr, const NbrList &L, bool indirect, const uint32_t *status,
+                           cudaStream_t st) {
+    if (indirect)
+        k_density<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, status);
+    else
+        k_density<false, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, status);
+}
+
+cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
+                           const float4 *vel, float4 *rp, float4 *fr, const NbrList &L,
+                           bool indirect, cudaStream_t st, int threads) {
+    const WalkCtx G = global_ctx(B, pos);
+    if (T.n) {
+        if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, indirect, B.status, st);
+        else density_launch<256>(T, G, vel, rp, fr, L, indirect, B.status, st);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_force(const StepParams &P, const SortBuffers &B, const float4 *pos,
-                         const float4 *vel, const float4 *rp, float4 *pos_out, float4 *vel_out,
-                         float4 *force_out, bool indirect, cudaStream_t st) {
-    const WalkCtx W = make_ctx(P, B, pos);
-    if (P.n) {
-        if (indirect)
-            k_force<true><<<blocks(P.n, kForceThreads), kForceThreads, 0, st>>>(
-                P, W, vel, rp, pos_out, vel_out, force_out, B.status);
+template <int kThreads>
+static void force_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel,
+                         const float4 *rp, const float4 *fr, const NbrList &L, float4 *pos_out,
+                         float4 *vel_out, float4 *force_out, bool indirect,
+                         const uint32_t *status, cudaStream_t st) {
+    if (indirect)
+        k_force<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, status);
+    else
+        k_force<false, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, status);
+}
+
+cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
+                         const float4 *vel, const float4 *rp, const float4 *fr, const NbrList &L,
+                         float4 *pos_out, float4 *vel_out, float4 *force_out, bool indirect,
+                         cudaStream_t st, int threads) {
+    const WalkCtx G = global_ctx(B, pos);
+    if (T.n) {
+        if (threads == 128)
+            force_launch<128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect, B.status, st);
         else
-            k_force<false><<<blocks(P.n, kForceThreads), kForceThreads, 0, st>>>(
-                P, W, vel, rp, pos_out, vel_out, force_out, B.status);
+            force_launch<256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect, B.status, st);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_digest(const StepParams &P, const SortBuffers &B, const float4 *pos,
+cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                           const uint32_t *id, uint32_t *count, uint64_t *digest, bool indirect,
                           cudaStream_t st) {
-    const WalkCtx W = make_ctx(P, B, pos);
-    if (P.n) {
+    const WalkCtx G = global_ctx(B, pos);
+    if (T.n) {
         if (indirect)
-            k_digest<true><<<blocks(P.n, 256), 256, 0, st>>>(P, W, id, count, digest, B.status);
+            k_digest<true><<<blocks(T.n, 256), 256, 0, st>>>(T, G, id, count, digest, B.status);
         else
-            k_digest<false><<<blocks(P.n, 256), 256, 0, st>>>(P, W, id, count, digest, B.status);
+            k_digest<false><<<blocks(T.n, 256), 256, 0, st>>>(T, G, id, count, digest, B.status);
     }
     return cudaGetLastError();
 }
 
-cudaError_t launch_upload(uint32_t n, const float *pos3, const float *vel3, float4 *pos,
-                          float4 *vel, uint32_t *id, cudaStream_t st) {
-    if (n) k_upload<<<blocks(n, 256), 256, 0, st>>>(n, pos3, vel3, pos, vel, id);
+cudaError_t launch_upload_rows(uint32_t first, uint32_t n, const float *pos3, const float *vel3,
+                               float4 *pos, float4 *vel, uint32_t *id, cudaStream_t st) {
+    if (n) k_upload_rows<<<blocks(n, 256), 256, 0, st>>>(first, n, pos3, vel3, pos, vel, id);
     return cudaGetLastError();
 }
 
-cudaError_t launch_read_field(uint32_t n, int field, const uint32_t *id, const float4 *v4,
+cudaError_t launch_lattice_rows(uint32_t first, const LatticeGen &L, float4 *pos, float4 *vel,
+                                uint32_t *id, cudaStream_t st) {
+    const uint32_t n = L.nx * L.ny * L.nz;
+    if (n) k_lattice_rows<<<blocks(n, 256), 256, 0, st>>>(first, L, pos, vel, id);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_read_rows(uint32_t first, uint32_t n, int field, const uint32_t *id,
+                             const float4 *v4, const float4 *rp, float *out, cudaStream_t st) {
+    if (n) k_read_rows<<<blocks(n, 256), 256, 0, st>>>(first, n, field, id, v4, rp, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_read_field(const SceneTable &T, int field, const uint32_t *id, const float4 *v4,
                               const float4 *rp, float *out, cudaStream_t st) {
-    if (n) k_read_field<<<blocks(n, 256), 256, 0, st>>>(n, field, id, v4, rp, out);
+    if (T.n) k_read_field<<<blocks(T.n, 256), 256, 0, st>>>(T, field, id, v4, rp, out);
     return cudaGetLastError();
 }
 
-cudaError_t launch_transforms(uint32_t n, float half_h, const uint32_t *id, const float4 *pos,
+cudaError_t launch_transforms(const SceneTable &T, const uint32_t *id, const float4 *pos,
                               float *out16, cudaStream_t st) {
-    if (n)
-        k_transforms<<<blocks(n, 256), 256, 0, st>>>(n, half_h, id, pos,
-                                                     reinterpret_cast<float4 *>(out16));
+    if (T.n)
+        k_transforms<<<blocks(T.n, 256), 256, 0, st>>>(T, id, pos, reinterpret_cast<float4 *>(out16));
     return cudaGetLastError();
 }
 
-cudaError_t launch_cells(uint32_t n, float h, const uint32_t *id, const float4 *pos, int *cells,
+cudaError_t launch_cells(const SceneTable &T, const uint32_t *id, const float4 *pos, int *cells,
                          uint16_t *hash, cudaStream_t st) {
-    if (n) k_cells<<<blocks(n, 256), 256, 0, st>>>(n, h, id, pos, cells, hash);
+    if (T.n) k_cells<<<blocks(T.n, 256), 256, 0, st>>>(T, id, pos, cells, hash);
     return cudaGetLastError();
 }
 

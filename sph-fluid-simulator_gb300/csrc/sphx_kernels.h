@@ -20,36 +20,77 @@ struct SortBuffers {
     uint32_t *start;     // slots + 1
     uint32_t *tile_sum;  // ceil((slots + 1) / 4096)
     uint32_t *status;    // 2 words: error bits, x-wrap flag (see below)
+    uint2 *large;        // cells longer than 64 queued for the block sort
+    uint32_t large_cap;  // entries of `large` (n / 64 + 2 suffices)
     uint32_t slots;      // gx * gy * gz
-    uint32_t max_cell;   // occupancy above which a step refuses to walk
+    uint32_t max_cell;   // occupancy above which a step refuses to walk (<= kLargeCell)
 };
 
+// Largest cell the step sorts (shared-memory bitonic sort of 8-byte keys) and
+// the CTAs that share the queued large cells.
+constexpr uint32_t kLargeCell = 16384;
+constexpr unsigned kLargeBlocks = 152;
+inline uint32_t large_list_cap(uint32_t n) { return n / 64 + 2; }
+
 // status[0]: sticky error bits; status[1]: set during a step's sort when a
-// particle lies outside the grid's x extent (cleared at each sort).
+// particle lies outside the grid's x extent; status[2]: number of large
+// cells queued (both cleared at each sort).
 constexpr uint32_t kStatusDomainBit = 1u;    // non-finite or |x/h| >= 2^30
 constexpr uint32_t kStatusOverflowBit = 2u;  // a cell above max_cell
 constexpr uint32_t kStatusErrorMask = 3u;
 
-cudaError_t launch_sort(const StepParams &P, const SortBuffers &B, const float4 *pos,
+cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                         cudaStream_t st);
+// Once per device before the first launch_sort (outside any stream capture):
+// allows the large-cell sort its shared memory.
+cudaError_t prepare_device();
 cudaError_t launch_gather(uint32_t n, const SortBuffers &B, const float4 *pos_in,
                           const float4 *vel_in, const uint32_t *id_in, float4 *pos_out,
                           float4 *vel_out, uint32_t *id_out, cudaStream_t st);
-cudaError_t launch_density(const StepParams &P, const SortBuffers &B, const float4 *pos,
-                           float4 *rp, bool indirect, cudaStream_t st);
-cudaError_t launch_force(const StepParams &P, const SortBuffers &B, const float4 *pos,
-                         const float4 *vel, const float4 *rp, float4 *pos_out, float4 *vel_out,
-                         float4 *force_out, bool indirect, cudaStream_t st);
-cudaError_t launch_digest(const StepParams &P, const SortBuffers &B, const float4 *pos,
+// Accepted-neighbour lists the density kernel records for the force kernel:
+// row k of particle i is nbr[k * stride + i] for k < min(count[i], 64); a
+// count above 64 means the force kernel walks for that particle.  nbr NULL:
+// nothing is recorded (the density pass alone).
+struct NbrList {
+    uint32_t *nbr;
+    uint32_t *count;
+    uint32_t stride;
+};
+constexpr uint32_t kNbrListSlots = 64;
+
+// fr: 2 float4 per particle, (x, y, z, p) and (vx, vy, vz, 1/rho), written
+// by the density kernel when L.nbr is set (vel then required).
+cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
+                           const float4 *vel, float4 *rp, float4 *fr, const NbrList &L,
+                           bool indirect, cudaStream_t st, int threads = 256);
+cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
+                         const float4 *vel, const float4 *rp, const float4 *fr, const NbrList &L,
+                         float4 *pos_out, float4 *vel_out, float4 *force_out, bool indirect,
+                         cudaStream_t st, int threads = 256);
+cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                           const uint32_t *id, uint32_t *count, uint64_t *digest, bool indirect,
                           cudaStream_t st);
-cudaError_t launch_upload(uint32_t n, const float *pos3, const float *vel3, float4 *pos,
-                          float4 *vel, uint32_t *id, cudaStream_t st);
-cudaError_t launch_read_field(uint32_t n, int field, const uint32_t *id, const float4 *v4,
+// Rows [first, first + n) from host-ordered staging (scene-local ids), and
+// back: one scene's rows to staging in its id order (field: 0 pos, 1 vel,
+// 2 force, 3 rho, 4 prs).
+cudaError_t launch_upload_rows(uint32_t first, uint32_t n, const float *pos3, const float *vel3,
+                               float4 *pos, float4 *vel, uint32_t *id, cudaStream_t st);
+// Dam-break lattice generated on the device into rows [first, first + n).
+struct LatticeGen {
+    uint32_t nx, ny, nz;
+    float origin[3];
+    float spacing, jitter;
+    uint64_t seed;
+};
+cudaError_t launch_lattice_rows(uint32_t first, const LatticeGen &L, float4 *pos, float4 *vel,
+                                uint32_t *id, cudaStream_t st);
+cudaError_t launch_read_rows(uint32_t first, uint32_t n, int field, const uint32_t *id,
+                             const float4 *v4, const float4 *rp, float *out, cudaStream_t st);
+cudaError_t launch_read_field(const SceneTable &T, int field, const uint32_t *id, const float4 *v4,
                               const float4 *rp, float *out, cudaStream_t st);
-cudaError_t launch_transforms(uint32_t n, float half_h, const uint32_t *id, const float4 *pos,
+cudaError_t launch_transforms(const SceneTable &T, const uint32_t *id, const float4 *pos,
                               float *out16, cudaStream_t st);
-cudaError_t launch_cells(uint32_t n, float h, const uint32_t *id, const float4 *pos, int *cells,
+cudaError_t launch_cells(const SceneTable &T, const uint32_t *id, const float4 *pos, int *cells,
                          uint16_t *hash, cudaStream_t st);
 
 // The reference's 60-byte Particle records (Particle.h:4-10) <-> resident state.

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstddef>
 #include <mutex>
 #include <string>
 
@@ -51,8 +52,11 @@ constexpr size_t kOffCount = kOffOrder + align256(4ull * kMaxParticles);
 constexpr size_t kOffStart = kOffCount + align256(4ull * (kSlots + 1));
 constexpr size_t kOffTiles = kOffStart + align256(4ull * (kSlots + 1));
 constexpr size_t kOffStatus = kOffTiles + align256(4ull * kTiles);
-constexpr size_t kOffRp = kOffStatus + 256;
-constexpr size_t kScratchBytes = kOffRp + 16ull * kMaxParticles;
+constexpr size_t kOffTable = kOffStatus + 256;  // StepParams + particle / slot offsets
+constexpr size_t kOffRp = kOffTable + 1024;
+constexpr size_t kOffLarge = kOffRp + 16ull * kMaxParticles;  // queued large cells
+constexpr size_t kScratchBytes = kOffLarge + 8ull * (kMaxParticles / 64 + 2);
+static_assert(sizeof(sphx::StepParams) + 16 <= 1024, "scene table fits its scratch slot");
 
 static __device__ __align__(256) uint4 g_scratch[kScratchBytes / sizeof(uint4)];
 
@@ -71,6 +75,9 @@ int scratch_address(char **out) {
         if (e != cudaSuccess)
             return sphx::fail(SPHX_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
         g_addr[dev] = static_cast<char *>(p);
+        const cudaError_t e2 = sphx::prepare_device();
+        if (e2 != cudaSuccess)
+            return sphx::fail(SPHX_ERR_CUDA, std::string("prepare_device: ") + cudaGetErrorString(e2));
     }
     *out = g_addr[dev];
     return SPHX_OK;
@@ -111,8 +118,21 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     P.gasConstant = d.gasConstant;
     P.restDensity = d.restDensity;
     P.mass = d.mass;
+    P.halfH = d.h / 2.f;
+    P.h2w = d.h * d.h * (1.0f + 3.814697265625e-06f);
     P.grid = sphx::Grid{kGridOrigin, kGridOrigin, kGridOrigin, kGridDim, kGridDim, kGridDim};
     P.n = (uint32_t)n;
+    // the one-scene table lives in the static array too: params, pofs {0, n}, sofs {0, slots}
+    struct {
+        sphx::StepParams p;
+        uint32_t pofs[2];
+        uint32_t sofs[2];
+    } tbl = {P, {0u, (uint32_t)n}, {0u, kSlots}};
+    char *dtbl = base + kOffTable;
+    const sphx::SceneTable T{reinterpret_cast<const sphx::StepParams *>(dtbl),
+                             reinterpret_cast<const uint32_t *>(dtbl + offsetof(decltype(tbl), pofs)),
+                             reinterpret_cast<const uint32_t *>(dtbl + offsetof(decltype(tbl), sofs)),
+                             1u, (uint32_t)n};
 
     sphx::SortBuffers B;
     B.key = reinterpret_cast<uint32_t *>(base + kOffKey);
@@ -122,8 +142,10 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     B.start = reinterpret_cast<uint32_t *>(base + kOffStart);
     B.tile_sum = reinterpret_cast<uint32_t *>(base + kOffTiles);
     B.status = reinterpret_cast<uint32_t *>(base + kOffStatus);
+    B.large = reinterpret_cast<uint2 *>(base + kOffLarge);
+    B.large_cap = kMaxParticles / 64 + 2;
     B.slots = kSlots;
-    B.max_cell = 1024;
+    B.max_cell = sphx::kLargeCell;
     float4 *rp = reinterpret_cast<float4 *>(base + kOffRp);
     const float4 *pos = static_cast<const float4 *>(d_pos4);
 
@@ -131,8 +153,10 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     // must start from zero.
     SPHX_CUDA(cudaMemsetAsync(B.count, 0, 4ull * (kSlots + 1), st));
     SPHX_CUDA(cudaMemsetAsync(B.status, 0, 16, st));
-    SPHX_CUDA(sphx::launch_sort(P, B, pos, st));
-    SPHX_CUDA(sphx::launch_density(P, B, pos, rp, /*indirect=*/true, st));
+    SPHX_CUDA(cudaMemcpyAsync(dtbl, &tbl, sizeof tbl, cudaMemcpyHostToDevice, st));
+    SPHX_CUDA(sphx::launch_sort(T, B, pos, st));
+    SPHX_CUDA(sphx::launch_density(T, B, pos, nullptr, rp, nullptr, sphx::NbrList{nullptr, nullptr, 0},
+                                   /*indirect=*/true, st));
     k_split_rho_prs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P.n, rp, d_rho, d_prs);
     SPHX_CUDA(cudaGetLastError());
 
@@ -142,6 +166,6 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     if (status & sphx::kStatusDomainBit)
         return fail(SPHX_ERR_DOMAIN, "a position is non-finite or |x/h| >= 2^30");
     if (status & sphx::kStatusOverflowBit)
-        return fail(SPHX_ERR_OVERFLOW, "a cell holds more than 1024 particles");
+        return fail(SPHX_ERR_OVERFLOW, "a cell holds more than 16384 particles");
     return SPHX_OK;
 }

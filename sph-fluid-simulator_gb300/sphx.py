@@ -56,7 +56,18 @@ class Box(C.Structure):
 class Options(C.Structure):
     _fields_ = [("reorder_interval", C.c_int), ("use_graph", C.c_int), ("device", C.c_int),
                 ("stream", C.c_void_p), ("grid_ymax", C.c_float), ("grid_dims", C.c_int * 3),
-                ("grid_origin", C.c_int * 3), ("max_cell_occupancy", C.c_uint32)]
+                ("grid_origin", C.c_int * 3), ("max_cell_occupancy", C.c_uint32),
+                ("density_threads", C.c_int), ("force_threads", C.c_int)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("settings", Settings), ("box", Box), ("n", C.c_size_t),
+                ("pos3", C.c_void_p), ("vel3", C.c_void_p)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("density_threads", C.c_int), ("force_threads", C.c_int),
+                ("reorder_interval", C.c_int), ("ms_per_step", C.c_double)]
 
 
 class LatticeDesc(C.Structure):
@@ -74,6 +85,28 @@ class DeviceView(C.Structure):
 class KernelTimes(C.Structure):
     _fields_ = [("sort_ms", C.c_double), ("density_ms", C.c_double), ("force_ms", C.c_double),
                 ("steps", C.c_uint64), ("launches", C.c_uint64)]
+
+
+class ServerOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("steps_per_tick", C.c_int),
+                ("max_scenes", C.c_int), ("dt", C.c_float), ("device", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("settings", Settings), ("box", Box), ("n", C.c_size_t), ("pos3", C.c_void_p),
+                ("vel3", C.c_void_p), ("nsteps", C.c_int)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int), ("steps_done", C.c_int), ("submit_s", C.c_double),
+                ("admit_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("ticks", C.c_uint64),
+                ("relayouts", C.c_uint64), ("particle_steps", C.c_uint64),
+                ("live_scenes", C.c_size_t), ("queued", C.c_size_t),
+                ("bytes_in_use", C.c_size_t), ("elapsed_s", C.c_double)]
 
 
 _lib = None
@@ -101,6 +134,17 @@ def lib():
         "sphx_lattice": (C.c_int, [P(LatticeDesc), vp]),
         "sphx_reference_scene": (C.c_int, [C.c_size_t, C.c_float, vp]),
         "sphx_create": (C.c_int, [P(Settings), P(Box), P(Options), C.c_size_t, vp, vp, P(vp)]),
+        "sphx_create_batch": (C.c_int, [P(SceneDesc), C.c_size_t, P(Options), P(vp)]),
+        "sphx_scene_count": (C.c_size_t, [vp]),
+        "sphx_create_lattice": (C.c_int, [P(Settings), P(Box), P(Options), P(LatticeDesc), P(vp)]),
+        "sphx_replace_scene": (C.c_int, [vp, C.c_size_t, P(SceneDesc), P(LatticeDesc)]),
+        "sphx_set_settings": (C.c_int, [vp, C.c_size_t, P(Settings), P(Box)]),
+        "sphx_scene_range": (C.c_int, [vp, C.c_size_t, P(C.c_size_t), P(C.c_size_t)]),
+        "sphx_read_scene": (C.c_int, [vp, C.c_size_t, vp, vp, vp, vp, vp]),
+        "sphx_get_tuning": (C.c_int, [vp, P(Tuning)]),
+        "sphx_set_tuning": (C.c_int, [vp, P(Tuning)]),
+        "sphx_autotune": (C.c_int, [vp, C.c_float, C.c_int, C.c_char_p, P(Tuning)]),
+        "sphx_density_static": (C.c_int, [P(Settings), vp, C.c_size_t, vp, vp, vp]),
         "sphx_destroy": (C.c_int, [vp]),
         "sphx_count": (C.c_size_t, [vp]),
         "sphx_set_state": (C.c_int, [vp, vp, vp]),
@@ -113,6 +157,14 @@ def lib():
         "sphx_device_state": (C.c_int, [vp, P(DeviceView)]),
         "sphx_update_particles": (C.c_int, [vp, vp, C.c_size_t, P(Settings), P(Box), C.c_float]),
         "sphx_update_particles_release": (C.c_int, []),
+        "sphx_server_options_default": (None, [P(ServerOptions)]),
+        "sphx_server_create": (C.c_int, [P(ServerOptions), P(vp)]),
+        "sphx_server_submit": (C.c_int, [vp, P(Request), P(C.c_uint64)]),
+        "sphx_server_status": (C.c_int, [vp, C.c_uint64, P(RequestStatus)]),
+        "sphx_server_wait": (C.c_int, [vp, C.c_uint64, C.c_double]),
+        "sphx_server_result": (C.c_int, [vp, C.c_uint64, vp, vp, vp, vp]),
+        "sphx_server_stats_get": (C.c_int, [vp, P(ServerStats)]),
+        "sphx_server_destroy": (C.c_int, [vp]),
         "sphx_set_profiling": (C.c_int, [vp, C.c_int]),
         "sphx_get_kernel_times": (C.c_int, [vp, P(KernelTimes)]),
     }
@@ -261,6 +313,25 @@ def release_update_particles():
     _check(lib().sphx_update_particles_release())
 
 
+def batch_scenes(count=512, seed=0, nmin=1000, nmax=65536):
+    """The batched workload: `count` dam-break blocks with particle counts
+    log-uniform in [nmin, nmax], block aspect ratios uniform in [0.5, 2],
+    gas constant uniform in [10, 40] and viscosity uniform in [0.5, 3]
+    (other constants as config_settings), each in a box 2.5 / 1.25 / 1.25
+    times its block edges.  Returns a list of (Settings, pos, Box)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        target = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        aspect = rng.uniform(0.5, 2.0, 3)
+        c = (target / aspect.prod()) ** (1.0 / 3.0)
+        nx, ny, nz = (max(2, int(round(c * a))) for a in aspect)
+        s = config_settings(gas_const=float(rng.uniform(10, 40)), viscosity=float(rng.uniform(0.5, 3)))
+        pos, box = dambreak(nx, ny, nz, seed=seed * 100003 + k)
+        out.append((s, pos, box))
+    return out
+
+
 # ------------------------------------------------------------------ scene handle
 
 class Scene:
@@ -278,6 +349,94 @@ class Scene:
         _check(lib().sphx_create(C.byref(s), C.byref(self.box), C.byref(self.options), n,
                                  _ptr(pos), _ptr(vel), C.byref(h)))
         self.h = h
+
+    @classmethod
+    def batch(cls, scenes, options=None):
+        """One handle over many scenes: scenes is a list of (Settings, pos, Box)
+        or (Settings, pos, Box, vel)."""
+        self = cls.__new__(cls)
+        self.options = options if options is not None else default_options()
+        keep = []
+        descs = (SceneDesc * len(scenes))()
+        for k, sc in enumerate(scenes):
+            s, pos, box = sc[0], _f32(sc[1]), sc[2]
+            vel = None if len(sc) < 4 or sc[3] is None else _f32(sc[3], len(pos))
+            keep += [pos, vel]
+            descs[k] = SceneDesc(s, box, len(pos), pos.ctypes.data,
+                                 None if vel is None else vel.ctypes.data)
+        h = C.c_void_p()
+        _check(lib().sphx_create_batch(descs, len(scenes), C.byref(self.options), C.byref(h)))
+        self.h = h
+        self.n = int(lib().sphx_count(h))
+        self.settings = None
+        self.box = None
+        return self
+
+    @classmethod
+    def from_lattice(cls, s, box, desc, options=None):
+        """A scene whose lattice (LatticeDesc) is generated on the device."""
+        self = cls.__new__(cls)
+        self.options = options if options is not None else default_options()
+        h = C.c_void_p()
+        _check(lib().sphx_create_lattice(C.byref(s), C.byref(box), C.byref(self.options),
+                                         C.byref(desc), C.byref(h)))
+        self.h = h
+        self.n = int(lib().sphx_count(h))
+        self.settings = s
+        self.box = box
+        return self
+
+    def replace_scene(self, k, s, box, pos=None, vel=None, lattice=None):
+        keep = []
+        if lattice is None:
+            pos = _f32(pos)
+            vel = None if vel is None else _f32(vel, len(pos))
+            keep = [pos, vel]
+            d = SceneDesc(s, box, len(pos), pos.ctypes.data, None if vel is None else vel.ctypes.data)
+            _check(lib().sphx_replace_scene(self.h, k, C.byref(d), None))
+        else:
+            d = SceneDesc(s, box, 0, None, None)
+            _check(lib().sphx_replace_scene(self.h, k, C.byref(d), C.byref(lattice)))
+        self.n = int(lib().sphx_count(self.h))
+        del keep
+
+    def set_settings(self, k, s, box=None):
+        _check(lib().sphx_set_settings(self.h, k, C.byref(s),
+                                       C.byref(box) if box is not None else None))
+
+    @property
+    def scene_count(self):
+        return int(lib().sphx_scene_count(self.h))
+
+    def scene_range(self, k):
+        first, count = C.c_size_t(), C.c_size_t()
+        _check(lib().sphx_scene_range(self.h, k, C.byref(first), C.byref(count)))
+        return first.value, count.value
+
+    def read_scene(self, k):
+        n = self.scene_range(k)[1]
+        out = {"pos": np.zeros((n, 3), np.float32), "vel": np.zeros((n, 3), np.float32),
+               "force": np.zeros((n, 3), np.float32), "rho": np.zeros(n, np.float32),
+               "prs": np.zeros(n, np.float32)}
+        _check(lib().sphx_read_scene(self.h, k, _ptr(out["pos"]), _ptr(out["vel"]),
+                                     _ptr(out["rho"]), _ptr(out["prs"]), _ptr(out["force"])))
+        return out
+
+    def tuning(self):
+        t = Tuning()
+        _check(lib().sphx_get_tuning(self.h, C.byref(t)))
+        return t
+
+    def set_tuning(self, density_threads=256, force_threads=256, reorder_interval=1):
+        t = Tuning(density_threads, force_threads, reorder_interval, 0.0)
+        _check(lib().sphx_set_tuning(self.h, C.byref(t)))
+
+    def autotune(self, dt=DT, trial_steps=4, cache_path=None):
+        t = Tuning()
+        _check(lib().sphx_autotune(self.h, dt, trial_steps,
+                                   None if cache_path is None else cache_path.encode(),
+                                   C.byref(t)))
+        return t
 
     def close(self):
         if self.h:
@@ -346,3 +505,66 @@ class Scene:
         t = KernelTimes()
         _check(lib().sphx_get_kernel_times(self.h, C.byref(t)))
         return t
+
+
+class Server:
+    """The continuous-batching request loop (sphx_server_*)."""
+
+    REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+
+    def __init__(self, budget_bytes=None, steps_per_tick=10, max_scenes=0, dt=DT, device=0):
+        o = ServerOptions()
+        lib().sphx_server_options_default(C.byref(o))
+        if budget_bytes is not None:
+            o.hbm_budget_bytes = int(budget_bytes)
+        o.steps_per_tick = steps_per_tick
+        o.max_scenes = max_scenes
+        o.dt = dt
+        o.device = device
+        h = C.c_void_p()
+        _check(lib().sphx_server_create(C.byref(o), C.byref(h)))
+        self.h = h
+        self.sizes = {}
+
+    def submit(self, s, box, pos, nsteps, vel=None):
+        pos = _f32(pos)
+        vel = None if vel is None else _f32(vel, len(pos))
+        q = Request(s, box, len(pos), pos.ctypes.data, None if vel is None else vel.ctypes.data,
+                    int(nsteps))
+        t = C.c_uint64()
+        _check(lib().sphx_server_submit(self.h, C.byref(q), C.byref(t)))
+        self.sizes[t.value] = len(pos)
+        return t.value
+
+    def status(self, ticket):
+        st = RequestStatus()
+        _check(lib().sphx_server_status(self.h, ticket, C.byref(st)))
+        return st
+
+    def wait(self, ticket, timeout=120.0):
+        _check(lib().sphx_server_wait(self.h, ticket, timeout))
+
+    def result(self, ticket):
+        n = self.sizes.pop(ticket)
+        out = {"pos": np.zeros((n, 3), np.float32), "vel": np.zeros((n, 3), np.float32),
+               "rho": np.zeros(n, np.float32), "prs": np.zeros(n, np.float32)}
+        _check(lib().sphx_server_result(self.h, ticket, _ptr(out["pos"]), _ptr(out["vel"]),
+                                        _ptr(out["rho"]), _ptr(out["prs"])))
+        return out
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().sphx_server_stats_get(self.h, C.byref(st)))
+        return st
+
+    def close(self):
+        if self.h:
+            lib().sphx_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+

@@ -121,4 +121,5 @@ def test_reference_presets(sphx_lib):
     assert (b.xmin, b.xmax, b.ymin, b.zmin, b.zmax, b.has_ceiling) == (-8, 8, 0, -8, 8, 0)
     assert np.float32(b.damping) == np.float32(0.5) and np.float32(b.offset) == np.float32(1e-4)
     o = sphx_lib.default_options()
-    assert o.reorder_interval == 1 and o.max_cell_occupancy == 1024
+    assert o.reorder_interval == 1 and o.max_cell_occupancy == 16384
+    assert o.density_threads == 256 and o.force_threads == 256
