@@ -282,6 +282,21 @@ def run_serve(a):
     print(json.dumps(line), flush=True)
 
 
+def run_steps_only(a):
+    """Profiling driver: the headline scene (or a --side^3 block), W + K steps
+    as plain launches (no graph, no events), one summary line."""
+    import torch
+    import sphx
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    pos, box = sphx.dambreak(a.side)
+    with sphx.Scene(sphx.config_settings(), box, pos, None,
+                    sphx.default_options(device=local, use_graph=0)) as sc:
+        sc.step(sphx.DT, a.warmup + a.steps)
+        sc.synchronize()
+    print(json.dumps({"workload": "steps", "particles": len(pos), "steps": a.warmup + a.steps}))
+
+
 def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -446,7 +461,8 @@ def main():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="sphx", choices=["sphx", "reference"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "steps"])
+    ap.add_argument("--side", type=int, default=SIDE, help="block side of --workload steps")
     ap.add_argument("--batch-steps", type=int, default=20,
                     help="steps of the batched-vs-sequential comparison in the plain run (0: skip)")
     ap.add_argument("--requests", type=int, default=32)
@@ -467,6 +483,8 @@ def main():
         run_batch(a)
     elif a.workload == "serve":
         run_serve(a)
+    elif a.workload == "steps":
+        run_steps_only(a)
     else:
         run_sphx(a)
 

@@ -26,10 +26,13 @@
 #include "sphx_kernels.h"
 
 // Resident threads per SM the two walk kernels are compiled for (register
-// cap 65536 / SPHX_WALK_THREADS_PER_SM); the block size is a template
-// parameter chosen per launch (128 or 256, see Tuning).
-#ifndef SPHX_WALK_THREADS_PER_SM
-#define SPHX_WALK_THREADS_PER_SM 1024
+// cap 65536 / threads); the block size is a template parameter chosen per
+// launch (128 or 256, see Tuning).
+#ifndef SPHX_DENSITY_THREADS_PER_SM
+#define SPHX_DENSITY_THREADS_PER_SM 1024
+#endif
+#ifndef SPHX_FORCE_THREADS_PER_SM
+#define SPHX_FORCE_THREADS_PER_SM 1024
 #endif
 
 namespace sphx {
@@ -559,16 +562,30 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 // the force kernel walks for it instead.
 constexpr uint32_t kNbrSlots = 64;
 
+// Optionally (SPHX_NBR_STAGED > 0) the first entries go to this thread's
+// column of a shared-memory list and are written out row by row at the end.
+// Off by default: on GB300 the shared memory it takes from L1 costs the
+// candidate loads more than the scattered list stores cost.
+#ifndef SPHX_NBR_STAGED
+#define SPHX_NBR_STAGED 0
+#endif
+constexpr uint32_t kNbrStaged = SPHX_NBR_STAGED;
+
 struct DensityVisitor {
     float h2;
     float acc, comp;  // compensated sum of (h^2 - r^2)^3
-    uint32_t *row;    // &nbr[i]
+    uint32_t *row;    // &nbr[i], or NULL: nothing recorded
     uint32_t stride;
+    uint32_t *stage;  // this thread's column of the staging list
+    uint32_t stage_stride;
     uint32_t cnt;
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float d2) {
         const float u = __fsub_rn(h2, d2);
         kahan_add(acc, comp, __fmul_rn(__fmul_rn(u, u), u));
-        if (row && cnt < kNbrSlots) row[cnt * stride] = j;
+        if (row) {
+            if (cnt < kNbrStaged) stage[cnt * stage_stride] = j;
+            else if (cnt < kNbrSlots) row[cnt * stride] = j;
+        }
         ++cnt;
     }
 };
@@ -590,9 +607,10 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
 }
 
 template <bool kInd, int kThreads>
-__global__ void __launch_bounds__(kThreads, SPHX_WALK_THREADS_PER_SM / kThreads)
+__global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
               float4 *__restrict__ fr, NbrList L, const uint32_t *__restrict__ status) {
+    __shared__ uint32_t s_stage[kNbrStaged > 0 ? kNbrStaged * kThreads : 1];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= T.n || (status[0] & kStatusErrorMask)) return;
     const uint32_t i = kInd ? G.order[t] : t;
@@ -602,13 +620,17 @@ __global__ void __launch_bounds__(kThreads, SPHX_WALK_THREADS_PER_SM / kThreads)
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
-    DensityVisitor v{P.h2, 0.f, 0.f, L.nbr ? L.nbr + i : nullptr, L.stride, 0u};
+    DensityVisitor v{P.h2, 0.f,     0.f, L.nbr ? L.nbr + i : nullptr, L.stride, s_stage + threadIdx.x,
+                     kThreads, 0u};
     walk<kInd>(W, s, i, pi, v);
     const float rho = __fadd_rn(__fmul_rn(P.mp6, v.acc), P.selfDens);
     const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
     const float inv = __frcp_rn(rho);
     rp[i] = make_float4(rho, prs, inv, 0.f);
     if (L.nbr) {
+        const uint32_t staged = min(v.cnt, kNbrStaged);
+#pragma unroll 1
+        for (uint32_t k = 0; k < staged; ++k) v.row[(size_t)k * L.stride] = v.stage[k * kThreads];
         L.count[i] = v.cnt;
         // what the force kernel reads of a neighbour, in one 32-byte record
         const float4 vi = vel[i];
@@ -646,10 +668,7 @@ struct ForcePair {
 };
 
 // r^2 of the reference (sph.cpp:57) from a neighbour's record, then the pair.
-__device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *__restrict__ fr,
-                                                 uint32_t j, float4 pi) {
-    const float4 a = fr[2 * (size_t)j];
-    const float4 b = fr[2 * (size_t)j + 1];
+__device__ __forceinline__ void pair_add_record(ForcePair &pair, float4 a, float4 b, float4 pi) {
     const float dx = __fsub_rn(a.x, pi.x);
     const float dy = __fsub_rn(a.y, pi.y);
     const float dz = __fsub_rn(a.z, pi.z);
@@ -657,11 +676,19 @@ __device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *
     pair.add(dx, dy, dz, d2, a.w, b);
 }
 
+__device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *__restrict__ fr,
+                                                 uint32_t j, float4 pi) {
+    pair_add_record(pair, fr[2 * (size_t)j], fr[2 * (size_t)j + 1], pi);
+}
+
 // The force walk in two phases: the candidate test only appends accepted
 // neighbours to this thread's column of a shared-memory list; the pair
 // math then runs over the list with every lane busy, instead of under the
 // acceptance branch (about 1 candidate in 4 passes) with most lanes idle.
-constexpr int kForceList = 48;  // list slots per thread (flushed when full)
+#ifndef SPHX_FORCE_LIST
+#define SPHX_FORCE_LIST 16
+#endif
+constexpr int kForceList = SPHX_FORCE_LIST;  // fallback list slots per thread (flushed when full)
 
 template <int kThreads>
 struct ForceListVisitor {
@@ -722,7 +749,7 @@ __device__ __forceinline__ void integrate(const StepParams &P, float4 &x, float4
 }
 
 template <bool kInd, int kThreads>
-__global__ void __launch_bounds__(kThreads, SPHX_WALK_THREADS_PER_SM / kThreads)
+__global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads)
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
@@ -741,8 +768,16 @@ __global__ void __launch_bounds__(kThreads, SPHX_WALK_THREADS_PER_SM / kThreads)
     const uint32_t cnt = L.count[i];
     if (cnt <= kNbrSlots) {  // the density kernel's list, same neighbours, same order
         const uint32_t *row = L.nbr + i;
+        uint32_t k = 0;
 #pragma unroll 1
-        for (uint32_t k = 0; k < cnt; ++k) pair_from_record(pair, fr, row[(size_t)k * L.stride], pi);
+        for (; k + 1 < cnt; k += 2) {  // both records in flight, then summed in list order
+            const uint32_t j0 = row[(size_t)k * L.stride], j1 = row[(size_t)(k + 1) * L.stride];
+            const float4 a0 = fr[2 * (size_t)j0], b0 = fr[2 * (size_t)j0 + 1];
+            const float4 a1 = fr[2 * (size_t)j1], b1 = fr[2 * (size_t)j1 + 1];
+            pair_add_record(pair, a0, b0, pi);
+            pair_add_record(pair, a1, b1, pi);
+        }
+        if (k < cnt) pair_from_record(pair, fr, row[(size_t)k * L.stride], pi);
     } else {
         WalkStart s;
         walk_start(P, pi, s);
