@@ -363,10 +363,26 @@ __device__ __forceinline__ void scan_run(const WalkCtx &W, uint32_t a, uint32_t 
 // When some particle lies outside the grid's x extent (xmono false) the run
 // is not monotone in x and candidates past xhi are skipped, not the rest of
 // the run.
+#ifndef SPHX_WINDOW_SEARCH
+#define SPHX_WINDOW_SEARCH 0
+#endif
+
 template <bool kInd, class V>
 __device__ __forceinline__ void scan_run_x(const WalkCtx &W, uint32_t a, uint32_t b, uint32_t self,
                                            float4 pi, float xlo, float xhi, bool xmono, V &vis) {
     uint32_t t = a;
+#if SPHX_WINDOW_SEARCH
+    if (xmono) {  // the run is x-sorted: binary search for the first x >= xlo
+        uint32_t lo = a, hi = b;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            const float x = W.pos[kInd ? W.order[mid] : mid].x;
+            if (x < xlo) lo = mid + 1;
+            else hi = mid;
+        }
+        t = lo;
+    }
+#endif
     for (; t + 1 < b; t += 2) {
         const uint32_t j0 = kInd ? W.order[t] : t;
         const uint32_t j1 = kInd ? W.order[t + 1] : t + 1;
@@ -429,8 +445,12 @@ __device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, in
     const Grid &g = W.grid;
     if (mx >= 1 && mx + 1 < g.gx) {
         const float h = W.h;
+#if SPHX_NO_YZ_NARROW
+        const float eym = 0.f, eyp = 0.f, ezm = 0.f, ezp = 0.f;
+#else
         const float eym = gap_to_cell(pi.y, c.cy, -1, h), eyp = gap_to_cell(pi.y, c.cy, 1, h);
         const float ezm = gap_to_cell(pi.z, c.cz, -1, h), ezp = gap_to_cell(pi.z, c.cz, 1, h);
+#endif
         const float ey2[3] = {eym * eym, 0.f, eyp * eyp};
         const float ez2[3] = {ezm * ezm, 0.f, ezp * ezp};
         uint32_t rows = 0;
@@ -583,7 +603,7 @@ struct DensityVisitor {
         const float u = __fsub_rn(h2, d2);
         kahan_add(acc, comp, __fmul_rn(__fmul_rn(u, u), u));
         if (row) {
-            if (cnt < kNbrStaged) stage[cnt * stage_stride] = j;
+            if ((int)cnt < (int)kNbrStaged) stage[cnt * stage_stride] = j;
             else if (cnt < kNbrSlots) row[cnt * stride] = j;
         }
         ++cnt;
