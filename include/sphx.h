@@ -67,6 +67,9 @@ typedef struct sphx_options {
     uint32_t max_cell_occupancy; /* particles per cell before a step fails (0 or > 16384: 16384) */
     int density_threads;   /* block size of the density kernel: 128 or 256 (0: 256) */
     int force_threads;     /* block size of the force kernel: 128 or 256 (0: 256) */
+    uint32_t neighbor_slots; /* accepted neighbours the density pass records per particle for
+                                the force pass (0: 256, at most 1024); particles with more are
+                                walked again by the force pass */
 } sphx_options;
 
 /* One scene of a batch: its settings, walls and initial host state. */
@@ -226,7 +229,7 @@ int sphx_update_particles_release(void);
  * device memory when they need the result (a plugin inside a frame with a
  * fixed GPU memory budget, or a host that gives the library buffers but no
  * right to call cudaMalloc).  Its scratch is one static device array of about
- * 5.5 MiB per GPU, held until the process exits; n may be at most 131,072
+ * 6.5 MiB per GPU, held until the process exits; n may be at most 131,072
  * (larger n: SPHX_ERR_INVALID).  Calls share that array, so calls whose work
  * overlaps on the GPU race.  The first call on a device looks up the array's
  * address; make it before any stream capture.  Synchronises `stream`. */

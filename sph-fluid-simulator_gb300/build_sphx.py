@@ -46,8 +46,9 @@ def _compile(src, extra=()):
     if src.endswith(".cu"):
         cmd = [NVCC, *NVCC_FLAGS, *extra, *inc, "-c", src, "-o", obj]
     else:
-        cmd = ["g++", *CXX_FLAGS, *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c", src,
-               "-o", obj]
+        defs = [e for e in extra if e.startswith("-D")]  # variant defines apply to host code too
+        cmd = ["g++", *CXX_FLAGS, *defs, *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c",
+               src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("compile failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))

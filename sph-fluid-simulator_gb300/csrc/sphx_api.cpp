@@ -136,20 +136,20 @@ struct Layout {
     enum {
         kPos0, kPos1, kVel0, kVel1, kId0, kId1, kRp, kForce, kKey, kRank, kOrder, kCount,
         kStart, kTiles, kStatus, kStaging, kParams, kPofs, kSofs, kLarge, kFr, kNbr, kNcount,
-        kNum
+        kScat, kNum
     };
     size_t off[kNum];
     size_t total;
 };
 
-Layout layout_for(size_t cn, size_t cs, size_t csc) {
+Layout layout_for(size_t cn, size_t cs, size_t csc, size_t slots) {
     const size_t ntiles = (cs + 1 + 4095) / 4096;
     const size_t sizes[Layout::kNum] = {16 * cn, 16 * cn, 16 * cn, 16 * cn, 4 * cn, 4 * cn,
                                         16 * cn, 16 * cn, 4 * cn, 4 * cn, 4 * cn,
                                         4 * (cs + 1), 4 * (cs + 1), 4 * ntiles, 256, 24 * cn,
                                         sizeof(sphx::StepParams) * csc, 4 * (csc + 1),
                                         4 * (csc + 1), 8ull * sphx::large_list_cap((uint32_t)cn),
-                                        32 * cn, 4ull * sphx::kNbrListSlots * cn, 4 * cn};
+                                        32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn};
     Layout L;
     size_t o = 0;
     for (int k = 0; k < Layout::kNum; ++k) {
@@ -173,6 +173,7 @@ void bind(sphx_handle *h, char *a, const Layout &L) {
     h->sb.key = (uint32_t *)(a + L.off[Layout::kKey]);
     h->sb.rank = (uint32_t *)(a + L.off[Layout::kRank]);
     h->sb.order = (uint32_t *)(a + L.off[Layout::kOrder]);
+    h->sb.scat = (uint2 *)(a + L.off[Layout::kScat]);
     h->sb.count = (uint32_t *)(a + L.off[Layout::kCount]);
     h->sb.start = (uint32_t *)(a + L.off[Layout::kStart]);
     h->sb.tile_sum = (uint32_t *)(a + L.off[Layout::kTiles]);
@@ -189,7 +190,7 @@ void bind(sphx_handle *h, char *a, const Layout &L) {
 
 // Allocates an arena for the capacities, zeroes its counts and status.
 int alloc_arena(sphx_handle *h, size_t cn, size_t cs, size_t csc, char **out, Layout *L) {
-    *L = layout_for(cn, cs, csc);
+    *L = layout_for(cn, cs, csc, h->opt.neighbor_slots);
     char *a = nullptr;
     if (cudaMalloc(&a, L->total) != cudaSuccess) {
         cudaGetLastError();
@@ -317,7 +318,7 @@ cudaError_t enqueue_step(sphx_handle *h, bool reorder, int &pv, int &idc, cudaEv
         idc ^= 1;
     }
     if (ev) cudaEventRecord(ev[1], st);
-    const sphx::NbrList L{h->nbr, h->ncount, h->cap_n};
+    const sphx::NbrList L{h->nbr, h->ncount, h->opt.neighbor_slots};
     if ((e = sphx::launch_density(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L, !reorder,
                                   st, h->tune.density_threads)) != cudaSuccess)
         return e;
@@ -454,6 +455,10 @@ int sphx::create_handle(const SceneInit *inits, size_t nscenes, const sphx_optio
     if (o.reorder_interval < 1) return fail(SPHX_ERR_INVALID, "reorder_interval must be >= 1");
     if (o.max_cell_occupancy == 0 || o.max_cell_occupancy > sphx::kLargeCell)
         o.max_cell_occupancy = sphx::kLargeCell;
+    if (o.neighbor_slots == 0) o.neighbor_slots = sphx::kNbrSlotsDefault;
+    if (o.neighbor_slots > sphx::kNbrSlotsMax)
+        return fail(SPHX_ERR_INVALID, "neighbor_slots must be at most 1024");
+    o.neighbor_slots = (o.neighbor_slots + 3u) & ~3u;  // 16-byte list rows
     uint64_t total_n = 0, total_slots = 0;
     std::vector<sphx::Scene> scenes(nscenes);
     for (size_t k = 0; k < nscenes; ++k) {

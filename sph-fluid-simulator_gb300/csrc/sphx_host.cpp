@@ -76,6 +76,7 @@ void sphx_options_default(sphx_options *o) {
     o->max_cell_occupancy = 16384;
     o->density_threads = 256;
     o->force_threads = 256;
+    o->neighbor_slots = 256;
 }
 
 int sphx_derive(const sphx_settings *s, sphx_derived *out) {

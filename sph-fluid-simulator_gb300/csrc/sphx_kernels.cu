@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "sphx_common.h"
 #include "sphx_kernels.h"
 
@@ -203,48 +205,50 @@ __global__ void k_scan_apply(uint32_t *__restrict__ count, uint32_t m,
     }
 }
 
-__global__ void k_scatter(uint32_t n, const uint32_t *__restrict__ key,
-                          const uint32_t *__restrict__ rank, const uint32_t *__restrict__ start,
-                          uint32_t *__restrict__ order, const uint32_t *__restrict__ status) {
+// Each cell's run in arrival order: (particle, x bits) pairs.
+__global__ void k_scatter(uint32_t n, const float4 *__restrict__ pos,
+                          const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
+                          const uint32_t *__restrict__ start, uint2 *__restrict__ scat,
+                          const uint32_t *__restrict__ status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (*status & kStatusOverflowBit)) return;
-    order[start[key[i]] + rank[i]] = i;
+    scat[start[key[i]] + rank[i]] = make_uint2(i, __float_as_uint(pos[i].x));
 }
 
-// The particle that arrived first in a cell sorts the cell's run by
-// (x, particle index): deterministic, and it makes every run of
-// x-consecutive cells sorted by x, which the walk's x window relies on.
-// Runs longer than kSmallCell (clumped fluid) are queued for
-// k_cellsort_large instead.
+// Each particle's place in its cell's run sorted by (x, particle index): the
+// number of run members before it in that order (a strict total order on
+// finite x, so the places form a permutation).  Sorting by x makes every run
+// of x-consecutive cells sorted by x, which the walk's x window relies on,
+// and the index makes the order, and hence every float sum, deterministic.
+// Runs longer than kSmallCell (clumped fluid) are queued, by the particle
+// that arrived first, for k_cellsort_large instead.
 constexpr uint32_t kSmallCell = 64;
 
 __global__ void k_cellsort(uint32_t n, const float4 *__restrict__ pos,
                            const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
-                           const uint32_t *__restrict__ start, uint32_t *__restrict__ order,
-                           uint32_t *__restrict__ status, uint2 *__restrict__ large,
-                           uint32_t large_cap) {
+                           const uint32_t *__restrict__ start, const uint2 *__restrict__ scat,
+                           uint32_t *__restrict__ order, uint32_t *__restrict__ status,
+                           uint2 *__restrict__ large, uint32_t large_cap) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || rank[i] != 0u || (status[0] & kStatusOverflowBit)) return;
+    if (i >= n || (status[0] & kStatusErrorMask)) return;
     const uint32_t k = key[i];
-    const uint32_t a = start[k], b = start[k + 1];
-    if (b - a > kSmallCell) {
-        const uint32_t slot = atomicAdd(&status[2], 1u);
-        if (slot < large_cap) large[slot] = make_uint2(a, b - a);
+    const uint32_t a = start[k], c = start[k + 1] - a;
+    if (c > kSmallCell) {
+        if (rank[i] == 0u) {
+            const uint32_t slot = atomicAdd(&status[2], 1u);
+            if (slot < large_cap) large[slot] = make_uint2(a, c);
+        }
         return;
     }
-    for (uint32_t x = a + 1; x < b; ++x) {
-        const uint32_t v = order[x];
-        const float vx = pos[v].x;
-        uint32_t y = x;
-        while (y > a) {
-            const uint32_t u = order[y - 1];
-            const float ux = pos[u].x;
-            if (!(ux > vx || (ux == vx && u > v))) break;
-            order[y] = u;
-            --y;
-        }
-        order[y] = v;
+    const float xi = pos[i].x;
+    uint32_t r = 0;
+#pragma unroll 4
+    for (uint32_t t = a; t < a + c; ++t) {
+        const uint2 e = scat[t];
+        const float xj = __uint_as_float(e.y);
+        r += (xj < xi || (xj == xi && e.x < i)) ? 1u : 0u;
     }
+    order[a + r] = i;
 }
 
 // Total order of floats as unsigned integers (finite values).
@@ -255,13 +259,13 @@ __device__ __forceinline__ uint32_t float_order(float f) {
 
 // One CTA per queued large cell: bitonic sort of (x, particle index) keys in
 // shared memory (up to kLargeCell entries), written back to the cell's run.
-__global__ void __launch_bounds__(512) k_cellsort_large(const float4 *__restrict__ pos,
+__global__ void __launch_bounds__(512) k_cellsort_large(const uint2 *__restrict__ scat,
                                                         uint32_t *__restrict__ order,
                                                         const uint32_t *__restrict__ status,
                                                         const uint2 *__restrict__ large,
                                                         uint32_t large_cap) {
     extern __shared__ unsigned long long skeys[];
-    if (status[0] & kStatusOverflowBit) return;
+    if (status[0] & kStatusErrorMask) return;
     const uint32_t count = min(status[2], large_cap);
     for (uint32_t c = blockIdx.x; c < count; c += gridDim.x) {
         const uint2 cell = large[c];  // (start, length), length <= kLargeCell
@@ -270,8 +274,8 @@ __global__ void __launch_bounds__(512) k_cellsort_large(const float4 *__restrict
         for (uint32_t t = threadIdx.x; t < m; t += blockDim.x) {
             unsigned long long v = ~0ull;
             if (t < cell.y) {
-                const uint32_t j = order[cell.x + t];
-                v = ((unsigned long long)float_order(pos[j].x) << 32) | j;
+                const uint2 e = scat[cell.x + t];
+                v = ((unsigned long long)float_order(__uint_as_float(e.y)) << 32) | e.x;
             }
             skeys[t] = v;
         }
@@ -303,7 +307,7 @@ __global__ void k_gather(uint32_t n, const uint32_t *__restrict__ order,
                          float4 *__restrict__ vel_out, uint32_t *__restrict__ id_out,
                          const uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n || (*status & kStatusOverflowBit)) return;
+    if (t >= n || (*status & kStatusErrorMask)) return;
     const uint32_t s = order[t];
     pos_out[t] = pos_in[s];
     vel_out[t] = vel_in[s];
@@ -564,6 +568,233 @@ __device__ __forceinline__ void walk(const WalkCtx &W, const WalkStart &s, uint3
         walk_slow<kInd>(W, s.c.cx, s.c.cy, s.c.cz, s.flags, self, pi, vis);
 }
 
+// Warp-cooperative form of the fast path.  Consecutive threads hold
+// consecutive cell-sorted particles, so most of a warp sits in one (y, z) row
+// of cells and shares its nine neighbour rows.  Lanes with the same scene and
+// row form a group; for each neighbour row the group copies the union of its
+// lanes' three-cell runs into this warp's shared-memory chunk (coalesced,
+// kCoopChunk particles at a time), then every lane scans its own run inside
+// the chunk with the same x window and early exit as scan_run_x.  The set of
+// pairs tested is exactly walk_rows'; only the loads are shared and the lanes
+// stay in step.  Lanes off the fast path (bucket collisions, the grid's x
+// seam) walk alone afterwards.
+//
+// What the chunk holds and how a lane scans its part of it is the scanner's
+// (PosScan: positions, for density and the digest; RecordScan: the force
+// kernel's 32-byte neighbour records).
+#ifndef SPHX_COOP_CHUNK
+#define SPHX_COOP_CHUNK 128
+#endif
+#ifndef SPHX_COOP_SEARCH
+#define SPHX_COOP_SEARCH 1
+#endif
+
+constexpr uint32_t kCoopChunk = SPHX_COOP_CHUNK;
+
+struct CoopLane {
+    bool valid;  // holds a particle that walks
+    bool fast;   // takes the cooperative path
+    uint64_t key;
+};
+
+__device__ __forceinline__ CoopLane coop_lane(bool valid, uint32_t sc, const WalkCtx &W,
+                                              const WalkStart &s) {
+    CoopLane c;
+    c.valid = valid;
+    c.fast = valid && s.flags == 0u && s.mx >= 1 && s.mx + 1 < W.grid.gx;
+    c.key = c.fast ? (((uint64_t)sc << 32) | ((uint32_t)s.mz * (uint32_t)W.grid.gy + (uint32_t)s.my))
+                   : ~0ull;
+    return c;
+}
+
+// One group's walk by its members alone (gmask): they load the chunks
+// between them and scan them.  For warps that are one group or a few large
+// ones (the common case: consecutive particles share a cell row).
+template <bool kInd, class S>
+__device__ __forceinline__ void coop_rows_group(const WalkCtx &W, const WalkStart &s, uint32_t self,
+                                                float4 pi, uint32_t gmask, uint32_t lane, S &scan) {
+    const float h = W.h;
+    const float eym = gap_to_cell(pi.y, s.c.cy, -1, h), eyp = gap_to_cell(pi.y, s.c.cy, 1, h);
+    const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
+    const float ey2[3] = {eym * eym, 0.f, eyp * eyp};
+    const float ez2[3] = {ezm * ezm, 0.f, ezp * ezp};
+    uint32_t rows = 0;
+#pragma unroll
+    for (int r = 0; r < 9; ++r)
+        if (W.h2w - ey2[r % 3] - ez2[r / 3] > 0.f) rows |= 1u << r;
+    const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
+    uint32_t todo = __reduce_or_sync(gmask, rows);
+    const uint32_t mxlo = __reduce_min_sync(gmask, (uint32_t)s.mx);
+    const uint32_t mxhi = __reduce_max_sync(gmask, (uint32_t)s.mx);
+    const uint32_t rank = __popc(gmask & ((1u << lane) - 1u)), gsize = __popc(gmask);
+#pragma unroll 1
+    while (todo) {
+        const int r = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const uint32_t base = row_base(W.grid, s.my, s.mz, r);
+        const uint32_t A = W.start[base + mxlo - 1], B = W.start[base + mxhi + 2];
+        const uint32_t a = W.start[base + s.mx - 1], b = W.start[base + s.mx + 2];
+        const int iy = r % 3, iz = r / 3;
+        const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
+        const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
+        bool done = !((rows >> r) & 1u) || a == b;
+        const float hx = done ? 0.f : fmaf(sqrtf(W.h2w - eyy - ezz), 1.0000009536743164f, xpad);
+        const float xlo = pi.x - hx, xhi = pi.x + hx;
+#pragma unroll 1
+        for (uint32_t c0 = A; c0 < B; c0 += S::kChunk) {
+            const uint32_t m = min(S::kChunk, B - c0);
+            for (uint32_t k = rank; k < m; k += gsize) scan.load(W, k, kInd ? W.order[c0 + k] : c0 + k);
+            __syncwarp(gmask);
+            if (!done && b > c0 && a < c0 + m)
+                done = scan.scan(W, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo, xhi, self, pi);
+            __syncwarp(gmask);
+        }
+    }
+}
+
+// One group's walk, every lane of the warp taking part: all of them load
+// the chunks, the members scan them.  For groups that are a few lanes of a
+// warp (particles of a clumped region among others).
+template <bool kInd, class S>
+__device__ __forceinline__ void coop_rows_warp(const WalkCtx &W, const WalkStart &s, uint32_t self,
+                                          float4 pi, bool member, uint32_t leader, uint32_t lane,
+                                          S &scan) {
+    float ey2[3] = {0.f, 0.f, 0.f}, ez2[3] = {0.f, 0.f, 0.f};
+    uint32_t rows = 0;
+    if (member) {
+        const float h = W.h;
+        const float eym = gap_to_cell(pi.y, s.c.cy, -1, h), eyp = gap_to_cell(pi.y, s.c.cy, 1, h);
+        const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
+        ey2[0] = eym * eym;
+        ey2[2] = eyp * eyp;
+        ez2[0] = ezm * ezm;
+        ez2[2] = ezp * ezp;
+#pragma unroll
+        for (int r = 0; r < 9; ++r)
+            if (W.h2w - ey2[r % 3] - ez2[r / 3] > 0.f) rows |= 1u << r;
+    }
+    const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
+    uint32_t todo = __reduce_or_sync(0xffffffffu, rows);
+    const uint32_t mxlo = __reduce_min_sync(0xffffffffu, member ? (uint32_t)s.mx : 0xffffffffu);
+    const uint32_t mxhi = __reduce_max_sync(0xffffffffu, member ? (uint32_t)s.mx : 0u);
+#pragma unroll 1
+    while (todo) {
+        const int r = __ffs(todo) - 1;
+        todo &= todo - 1;
+        uint32_t A = 0, B = 0, a = 0, b = 0;
+        if (member) {
+            const uint32_t base = row_base(W.grid, s.my, s.mz, r);
+            A = W.start[base + mxlo - 1];
+            B = W.start[base + mxhi + 2];
+            a = W.start[base + s.mx - 1];
+            b = W.start[base + s.mx + 2];
+        }
+        A = __shfl_sync(0xffffffffu, A, leader);
+        B = __shfl_sync(0xffffffffu, B, leader);
+        const int iy = r % 3, iz = r / 3;
+        const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
+        const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
+        bool done = !member || !((rows >> r) & 1u) || a == b;
+        const float hx = done ? 0.f : fmaf(sqrtf(W.h2w - eyy - ezz), 1.0000009536743164f, xpad);
+        const float xlo = pi.x - hx, xhi = pi.x + hx;
+#pragma unroll 1
+        for (uint32_t c0 = A; c0 < B; c0 += S::kChunk) {
+            const uint32_t m = min(S::kChunk, B - c0);
+            for (uint32_t k = lane; k < m; k += 32u) scan.load(W, k, kInd ? W.order[c0 + k] : c0 + k);
+            __syncwarp();
+            if (!done && b > c0 && a < c0 + m)
+                done = scan.scan(W, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo, xhi, self, pi);
+            __syncwarp();
+        }
+    }
+}
+
+// Runs the scanner over every fast lane's neighbours, one group after
+// another (kWarpLoad: coop_rows_warp, else coop_rows_group); the lanes off
+// the fast path then walk alone with `vis`.  Every lane of the warp calls it
+// (lanes without a walk pass valid = false).
+template <bool kInd, bool kWarpLoad, class S, class V>
+__device__ __forceinline__ void coop_walk(const WalkCtx &W, const WalkStart &s, const CoopLane &cl,
+                                          uint32_t self, float4 pi, S &scan, V &vis) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t gm = __match_any_sync(0xffffffffu, cl.key);
+    uint32_t pending = __ballot_sync(0xffffffffu, cl.fast);
+#pragma unroll 1
+    while (pending) {
+        const uint32_t leader = __ffs(pending) - 1;
+        if (kWarpLoad) {
+            const uint32_t gmask = __shfl_sync(0xffffffffu, gm, leader);
+            coop_rows_warp<kInd>(W, s, self, pi, cl.fast && ((gmask >> lane) & 1u), leader, lane,
+                                 scan);
+            pending &= ~gmask;
+        } else {
+            if (cl.fast && ((gm >> leader) & 1u)) coop_rows_group<kInd>(W, s, self, pi, gm, lane, scan);
+            pending &= ~__shfl_sync(0xffffffffu, gm, leader);
+        }
+    }
+    if (cl.valid && !cl.fast) walk<kInd>(W, s, self, pi, vis);
+}
+
+// Chunk of candidate positions; the lane's visitor sees each candidate of its
+// run inside the x window (scan_run_x's test, same order).
+// Chunk of candidate positions; the lane's visitor sees each candidate of
+// its run inside the x window (scan_run_x's test, same order).
+template <bool kInd>
+struct PosSmem {
+    float4 pos[kCoopChunk];
+    __device__ __forceinline__ float px(uint32_t k) const { return pos[k].x; }
+    __device__ __forceinline__ float4 p(uint32_t k) const { return pos[k]; }
+    __device__ __forceinline__ void put(uint32_t k, float4 v) { pos[k] = v; }
+    uint32_t idx[kInd ? kCoopChunk : 1];
+};
+
+template <bool kInd, class V>
+struct PosScan {
+    static constexpr uint32_t kChunk = kCoopChunk;
+    PosSmem<kInd> &sm;
+    V &vis;
+    __device__ __forceinline__ void load(const WalkCtx &W, uint32_t k, uint32_t j) {
+        sm.put(k, W.pos[j]);
+        if (kInd) sm.idx[k] = j;
+    }
+    __device__ __forceinline__ void test(const WalkCtx &W, uint32_t c0, uint32_t k, uint32_t self,
+                                         float4 pi) {
+        test_pair(W, kInd ? sm.idx[k] : c0 + k, sm.p(k), self, pi, 1u, vis);
+    }
+    // Chunk slots [lo, hi), the chunk starting at cell-sorted slot c0; true
+    // once past the window's end.
+    __device__ __forceinline__ bool scan(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
+                                         float xlo, float xhi, uint32_t self, float4 pi) {
+        if (!W.xmono) {  // runs not x-sorted this step: test the window bounds one by one
+            for (uint32_t k = lo; k < hi; ++k) {
+                const float4 p = sm.p(k);
+                if (p.x >= xlo && p.x <= xhi)
+                    test_pair(W, kInd ? sm.idx[k] : c0 + k, p, self, pi, 1u, vis);
+            }
+            return false;
+        }
+#if SPHX_COOP_SEARCH
+        {  // x-sorted: start at the first x >= xlo
+            uint32_t l = lo, u = hi;
+            while (l < u) {
+                const uint32_t mid = (l + u) >> 1;
+                if (sm.px(mid) < xlo) l = mid + 1;
+                else u = mid;
+            }
+            lo = l;
+        }
+#endif
+        uint32_t k = lo;
+#pragma unroll 2
+        for (; k < hi; ++k) {
+            const float4 p = sm.p(k);
+            if (p.x > xhi) return true;
+            if (p.x >= xlo) test_pair(W, kInd ? sm.idx[k] : c0 + k, p, self, pi, 1u, vis);
+        }
+        return false;
+    }
+};
+
 // ---------------------------------------------------------------- physics
 
 // Compensated (Kahan) accumulation: the GPU sums the same terms as the
@@ -577,35 +808,20 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 }
 
 // Accepted neighbours of a particle, in walk order, are also recorded for
-// the force kernel: list row k of particle i is nbr[k * stride + i], k <
-// kNbrSlots; a particle with more (clumped fluid) stores its count only and
-// the force kernel walks for it instead.
-constexpr uint32_t kNbrSlots = 64;
-
-// Optionally (SPHX_NBR_STAGED > 0) the first entries go to this thread's
-// column of a shared-memory list and are written out row by row at the end.
-// Off by default: on GB300 the shared memory it takes from L1 costs the
-// candidate loads more than the scattered list stores cost.
-#ifndef SPHX_NBR_STAGED
-#define SPHX_NBR_STAGED 0
-#endif
-constexpr uint32_t kNbrStaged = SPHX_NBR_STAGED;
-
+// the force kernel: entry k of particle i is nbr[i * slots + k], k < slots
+// (one contiguous row per particle, written by one lane front to back); a
+// particle with more (clumped fluid) stores its count only and the force
+// kernel walks for it instead.
 struct DensityVisitor {
     float h2;
     float acc, comp;  // compensated sum of (h^2 - r^2)^3
-    uint32_t *row;    // &nbr[i], or NULL: nothing recorded
-    uint32_t stride;
-    uint32_t *stage;  // this thread's column of the staging list
-    uint32_t stage_stride;
+    uint32_t *row;    // &nbr[i * slots], or NULL: nothing recorded
+    uint32_t slots;
     uint32_t cnt;
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float d2) {
         const float u = __fsub_rn(h2, d2);
         kahan_add(acc, comp, __fmul_rn(__fmul_rn(u, u), u));
-        if (row) {
-            if ((int)cnt < (int)kNbrStaged) stage[cnt * stage_stride] = j;
-            else if (cnt < kNbrSlots) row[cnt * stride] = j;
-        }
+        if (row && cnt < slots) row[cnt] = j;
         ++cnt;
     }
 };
@@ -626,32 +842,41 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
     return W;
 }
 
+#ifndef SPHX_DENSITY_COOP
+#define SPHX_DENSITY_COOP 1
+#endif
+
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
               float4 *__restrict__ fr, NbrList L, const uint32_t *__restrict__ status) {
-    __shared__ uint32_t s_stage[kNbrStaged > 0 ? kNbrStaged * kThreads : 1];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= T.n || (status[0] & kStatusErrorMask)) return;
-    const uint32_t i = kInd ? G.order[t] : t;
-    const uint32_t sc = scene_of(T, i);
+    // whole warps leave together: the cooperative walk needs every lane
+    if ((t & ~31u) >= T.n || (status[0] & kStatusErrorMask)) return;
+    const bool valid = t < T.n;
+    const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
+    const uint32_t sc = valid ? scene_of(T, i) : 0u;
     const StepParams &P = T.params[sc];
     const WalkCtx W = walk_ctx(T, G, sc, P, status);
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
-    DensityVisitor v{P.h2, 0.f,     0.f, L.nbr ? L.nbr + i : nullptr, L.stride, s_stage + threadIdx.x,
-                     kThreads, 0u};
-    walk<kInd>(W, s, i, pi, v);
+    DensityVisitor v{P.h2, 0.f, 0.f, valid && L.nbr ? L.nbr + (size_t)i * L.slots : nullptr, L.slots,
+                     0u};
+#if SPHX_DENSITY_COOP
+    __shared__ PosSmem<kInd> s_coop[kThreads / 32];
+    PosScan<kInd, DensityVisitor> scan{s_coop[threadIdx.x >> 5], v};
+    coop_walk<kInd, false>(W, s, coop_lane(valid, sc, W, s), i, pi, scan, v);
+#else
+    if (valid) walk<kInd>(W, s, i, pi, v);
+#endif
+    if (!valid) return;
     const float rho = __fadd_rn(__fmul_rn(P.mp6, v.acc), P.selfDens);
     const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
     const float inv = __frcp_rn(rho);
     rp[i] = make_float4(rho, prs, inv, 0.f);
-    if (L.nbr) {
-        const uint32_t staged = min(v.cnt, kNbrStaged);
-#pragma unroll 1
-        for (uint32_t k = 0; k < staged; ++k) v.row[(size_t)k * L.stride] = v.stage[k * kThreads];
-        L.count[i] = v.cnt;
+    if (L.nbr) L.count[i] = v.cnt;
+    if (fr) {
         // what the force kernel reads of a neighbour, in one 32-byte record
         const float4 vi = vel[i];
         fr[2 * (size_t)i] = make_float4(pi.x, pi.y, pi.z, prs);
@@ -701,30 +926,72 @@ __device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *
     pair_add_record(pair, fr[2 * (size_t)j], fr[2 * (size_t)j + 1], pi);
 }
 
-// The force walk in two phases: the candidate test only appends accepted
-// neighbours to this thread's column of a shared-memory list; the pair
-// math then runs over the list with every lane busy, instead of under the
-// acceptance branch (about 1 candidate in 4 passes) with most lanes idle.
-#ifndef SPHX_FORCE_LIST
-#define SPHX_FORCE_LIST 16
+// Force walk over a chunk of neighbour records (RecordScan): a lane first
+// tests up to 32 candidates of its run and marks the accepted ones in a bit
+// mask, then adds the marked pairs; the pair math thus runs with the lanes in
+// step instead of under the acceptance branch (about one candidate in four
+// passes), and every operand comes from shared memory.
+#ifndef SPHX_FORCE_CHUNK
+#define SPHX_FORCE_CHUNK 64
 #endif
-constexpr int kForceList = SPHX_FORCE_LIST;  // fallback list slots per thread (flushed when full)
 
-template <int kThreads>
-struct ForceListVisitor {
-    uint32_t *list;  // this thread's column: list[k * kThreads]
-    uint32_t cnt;
+template <bool kInd>
+struct RecordSmem {
+    float4 a[SPHX_FORCE_CHUNK];  // x, y, z, pressure
+    float4 b[SPHX_FORCE_CHUNK];  // vx, vy, vz, 1/density
+    uint32_t idx[kInd ? SPHX_FORCE_CHUNK : 1];
+};
+
+template <bool kInd>
+struct RecordScan {
+    static constexpr uint32_t kChunk = SPHX_FORCE_CHUNK;
+    RecordSmem<kInd> &sm;
+    const float4 *__restrict__ fr;
+    ForcePair &pair;
+    __device__ __forceinline__ void load(const WalkCtx &, uint32_t k, uint32_t j) {
+        sm.a[k] = fr[2 * (size_t)j];
+        sm.b[k] = fr[2 * (size_t)j + 1];
+        if (kInd) sm.idx[k] = j;
+    }
+    __device__ __forceinline__ bool scan(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
+                                         float xlo, float xhi, uint32_t self, float4 pi) {
+        bool done = false;
+#pragma unroll 1
+        for (uint32_t k0 = lo; k0 < hi && !done; k0 += 32) {
+            const uint32_t k1 = min(hi, k0 + 32);
+            uint32_t acc = 0;
+            for (uint32_t k = k0; k < k1; ++k) {
+                const float4 p = sm.a[k];
+                if (p.x > xhi) {
+                    if (W.xmono) { done = true; break; }
+                    continue;
+                }
+                if (p.x < xlo) continue;
+                const float dx = __fsub_rn(p.x, pi.x);
+                const float dy = __fsub_rn(p.y, pi.y);
+                const float dz = __fsub_rn(p.z, pi.z);
+                const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                const uint32_t j = kInd ? sm.idx[k] : c0 + k;
+                if (d2 < W.h2 && j != self) acc |= 1u << (k - k0);
+            }
+#pragma unroll 1
+            while (acc) {
+                const uint32_t k = k0 + __ffs(acc) - 1;
+                acc &= acc - 1;
+                pair_add_record(pair, sm.a[k], sm.b[k], pi);
+            }
+        }
+        return done;
+    }
+};
+
+// Lanes off the fast path add each accepted pair as the walk finds it.
+struct ForceVisitor {
+    ForcePair &pair;
     const float4 *__restrict__ fr;
     float4 pi;
-    ForcePair pair;
-    __device__ __forceinline__ void flush() {
-#pragma unroll 1
-        for (uint32_t k = 0; k < cnt; ++k) pair_from_record(pair, fr, list[k * kThreads], pi);
-        cnt = 0;
-    }
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float) {
-        list[cnt * kThreads] = j;
-        if (++cnt == (uint32_t)kForceList) flush();
+        pair_from_record(pair, fr, j, pi);
     }
 };
 
@@ -768,49 +1035,82 @@ __device__ __forceinline__ void integrate(const StepParams &P, float4 &x, float4
     }
 }
 
+// Force output, integration and the next state of particle i.
+__device__ __forceinline__ void force_finish(const StepParams &P, uint32_t i, float4 pi, float4 vi,
+                                             float rho, const ForcePair &pair,
+                                             float4 *__restrict__ pos_out,
+                                             float4 *__restrict__ vel_out,
+                                             float4 *__restrict__ force_out) {
+    const float fx = pair.fx, fy = pair.fy, fz = pair.fz;
+    force_out[i] = make_float4(fx, fy, fz, 0.f);
+    integrate(P, pi, vi, fx, fy, fz, rho);
+    pos_out[i] = pi;
+    vel_out[i] = vi;
+}
+
+// Force of every particle: over its list when its neighbours fit one (same
+// neighbours, same order as the density walk), else by a warp-cooperative
+// walk over the neighbour records in that same order.  Only the lanes past
+// their list take part in the walk, the whole warp loading for them.
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads)
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
             const uint32_t *__restrict__ status) {
-    __shared__ uint32_t s_list[kForceList * kThreads];
+    __shared__ RecordSmem<kInd> s_coop[kThreads / 32];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= T.n || (status[0] & kStatusErrorMask)) return;
-    const uint32_t i = kInd ? G.order[t] : t;
-    const uint32_t sc = scene_of(T, i);
+    // whole warps leave together: the cooperative walk needs every lane
+    if ((t & ~31u) >= T.n || (status[0] & kStatusErrorMask)) return;
+    const bool valid = t < T.n;
+    const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
+    const uint32_t sc = valid ? scene_of(T, i) : 0u;
     const StepParams &P = T.params[sc];
-    const WalkCtx W = walk_ctx(T, G, sc, P, status);
-    float4 pi = W.pos[i];
-    float4 vi = vel[i];
+    const float4 pi = G.pos[i];
+    const float4 vi = vel[i];
     const float4 q = rp[i];
     ForcePair pair{vi, q.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const uint32_t cnt = L.count[i];
-    if (cnt <= kNbrSlots) {  // the density kernel's list, same neighbours, same order
-        const uint32_t *row = L.nbr + i;
-        uint32_t k = 0;
+    const uint32_t cnt = valid ? L.count[i] : 0u;
+    if (cnt <= L.slots) {
+        // the row is 16-byte aligned (slots is a multiple of 4): four entries
+        // per load; entries past cnt in the last load are never used
+        const uint4 *row = reinterpret_cast<const uint4 *>(L.nbr + (size_t)i * L.slots);
 #pragma unroll 1
-        for (; k + 1 < cnt; k += 2) {  // both records in flight, then summed in list order
-            const uint32_t j0 = row[(size_t)k * L.stride], j1 = row[(size_t)(k + 1) * L.stride];
-            const float4 a0 = fr[2 * (size_t)j0], b0 = fr[2 * (size_t)j0 + 1];
-            const float4 a1 = fr[2 * (size_t)j1], b1 = fr[2 * (size_t)j1 + 1];
-            pair_add_record(pair, a0, b0, pi);
-            pair_add_record(pair, a1, b1, pi);
+        for (uint32_t k = 0; k < cnt; k += 4) {
+            const uint4 e = row[k >> 2];
+            const uint32_t left = cnt - k;
+            {  // two records in flight, then summed in list order
+                const uint32_t j1 = left > 1 ? e.y : e.x;
+                const float4 a0 = fr[2 * (size_t)e.x], b0 = fr[2 * (size_t)e.x + 1];
+                const float4 a1 = fr[2 * (size_t)j1], b1 = fr[2 * (size_t)j1 + 1];
+                pair_add_record(pair, a0, b0, pi);
+                if (left > 1) pair_add_record(pair, a1, b1, pi);
+            }
+            if (left > 2) {
+                const uint32_t j3 = left > 3 ? e.w : e.z;
+                const float4 a2 = fr[2 * (size_t)e.z], b2 = fr[2 * (size_t)e.z + 1];
+                const float4 a3 = fr[2 * (size_t)j3], b3 = fr[2 * (size_t)j3 + 1];
+                pair_add_record(pair, a2, b2, pi);
+                if (left > 3) pair_add_record(pair, a3, b3, pi);
+            }
         }
-        if (k < cnt) pair_from_record(pair, fr, row[(size_t)k * L.stride], pi);
-    } else {
+    }
+    const bool walker = valid && cnt > L.slots;
+    if (__any_sync(0xffffffffu, walker)) {
+        const WalkCtx W = walk_ctx(T, G, sc, P, status);
         WalkStart s;
         walk_start(P, pi, s);
-        ForceListVisitor<kThreads> v{s_list + threadIdx.x, 0u, fr, pi, pair};
-        walk<kInd>(W, s, i, pi, v);
-        v.flush();
-        pair = v.pair;
+        RecordScan<kInd> scan{s_coop[threadIdx.x >> 5], fr, pair};
+        ForceVisitor v{pair, fr, pi};
+        coop_walk<kInd, true>(W, s, coop_lane(walker, sc, W, s), i, pi, scan, v);
     }
+    if (!valid) return;
     const float fx = pair.fx, fy = pair.fy, fz = pair.fz;
     force_out[i] = make_float4(fx, fy, fz, 0.f);
-    integrate(P, pi, vi, fx, fy, fz, q.x);
-    pos_out[i] = pi;
-    vel_out[i] = vi;
+    float4 x = pi, v = vi;
+    integrate(P, x, v, fx, fy, fz, q.x);
+    pos_out[i] = x;
+    vel_out[i] = v;
 }
 
 // ---------------------------------------------------------------- readouts
@@ -832,21 +1132,28 @@ struct DigestVisitor {
     }
 };
 
+constexpr int kDigestThreads = 256;
+
 template <bool kInd>
 __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ id,
                          uint32_t *__restrict__ count_out, uint64_t *__restrict__ digest_out,
                          const uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= T.n || (status[0] & kStatusErrorMask)) return;
-    const uint32_t i = kInd ? G.order[t] : t;
-    const uint32_t sc = scene_of(T, i);
+    if ((t & ~31u) >= T.n || (status[0] & kStatusErrorMask)) return;
+    const bool valid = t < T.n;
+    const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
+    const uint32_t sc = valid ? scene_of(T, i) : 0u;
     const StepParams &P = T.params[sc];
     const WalkCtx W = walk_ctx(T, G, sc, P, status);
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
     DigestVisitor v{id, 0u, 0ull};
-    walk<kInd>(W, s, i, pi, v);
+    // the same walk as k_density's
+    __shared__ PosSmem<kInd> s_coop[kDigestThreads / 32];
+    PosScan<kInd, DigestVisitor> scan{s_coop[threadIdx.x >> 5], v};
+    coop_walk<kInd, false>(W, s, coop_lane(valid, sc, W, s), i, pi, scan, v);
+    if (!valid) return;
     const uint32_t d = T.pofs[sc] + id[i];
     count_out[d] = v.count;
     digest_out[d] = v.sum;
@@ -1041,10 +1348,10 @@ cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 
     k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(B.tile_sum, ntiles);
     k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.start);
     if (n) {
-        k_scatter<<<blocks(n, bs), bs, 0, st>>>(n, B.key, B.rank, B.start, B.order, B.status);
-        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.order,
+        k_scatter<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.scat, B.status);
+        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.scat, B.order,
                                                  B.status, B.large, B.large_cap);
-        k_cellsort_large<<<kLargeBlocks, 512, 8 * kLargeCell, st>>>(pos, B.order, B.status,
+        k_cellsort_large<<<kLargeBlocks, 512, 8 * kLargeCell, st>>>(B.scat, B.order, B.status,
                                                                     B.large, B.large_cap);
     }
     return cudaGetLastError();
@@ -1126,9 +1433,9 @@ cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float
     const WalkCtx G = global_ctx(B, pos);
     if (T.n) {
         if (indirect)
-            k_digest<true><<<blocks(T.n, 256), 256, 0, st>>>(T, G, id, count, digest, B.status);
+            k_digest<true><<<blocks(T.n, kDigestThreads), kDigestThreads, 0, st>>>(T, G, id, count, digest, B.status);
         else
-            k_digest<false><<<blocks(T.n, 256), 256, 0, st>>>(T, G, id, count, digest, B.status);
+            k_digest<false><<<blocks(T.n, kDigestThreads), kDigestThreads, 0, st>>>(T, G, id, count, digest, B.status);
     }
     return cudaGetLastError();
 }

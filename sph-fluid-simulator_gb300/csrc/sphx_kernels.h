@@ -16,6 +16,7 @@ struct SortBuffers {
     uint32_t *key;       // n: slot of each particle
     uint32_t *rank;      // n: arrival rank within its slot
     uint32_t *order;     // n: particle (data index) at each cell-sorted slot
+    uint2 *scat;         // n: (particle, x bits) of each slot in arrival order
     uint32_t *count;     // slots + 1
     uint32_t *start;     // slots + 1
     uint32_t *tile_sum;  // ceil((slots + 1) / 4096)
@@ -48,15 +49,15 @@ cudaError_t launch_gather(uint32_t n, const SortBuffers &B, const float4 *pos_in
                           const float4 *vel_in, const uint32_t *id_in, float4 *pos_out,
                           float4 *vel_out, uint32_t *id_out, cudaStream_t st);
 // Accepted-neighbour lists the density kernel records for the force kernel:
-// row k of particle i is nbr[k * stride + i] for k < min(count[i], 64); a
-// count above 64 means the force kernel walks for that particle.  nbr NULL:
-// nothing is recorded (the density pass alone).
+// entry k of particle i is nbr[i * slots + k] for k < min(count[i], slots),
+// slots a multiple of 4; a count above `slots` means the force kernel walks
+// for that particle.  nbr NULL: nothing is recorded (the density pass alone).
 struct NbrList {
     uint32_t *nbr;
     uint32_t *count;
-    uint32_t stride;
+    uint32_t slots;
 };
-constexpr uint32_t kNbrListSlots = 64;
+constexpr uint32_t kNbrSlotsDefault = 256, kNbrSlotsMax = 1024;
 
 // fr: 2 float4 per particle, (x, y, z, p) and (vx, vy, vz, 1/rho), written
 // by the density kernel when L.nbr is set (vel then required).

@@ -16,7 +16,7 @@
 // Limits and sharing:
 //   * at most kMaxParticles (131,072) particles per call; more is rejected
 //     with SPHX_ERR_INVALID;
-//   * the array (about 5.5 MiB) lives in every GPU that loads the library
+//   * the array (about 6.5 MiB) lives in every GPU that loads the library
 //     until the process exits;
 //   * every call on a device uses the same array, which keeps the previous
 //     call's contents: the counts and status words are cleared at the start
@@ -55,7 +55,8 @@ constexpr size_t kOffStatus = kOffTiles + align256(4ull * kTiles);
 constexpr size_t kOffTable = kOffStatus + 256;  // StepParams + particle / slot offsets
 constexpr size_t kOffRp = kOffTable + 1024;
 constexpr size_t kOffLarge = kOffRp + 16ull * kMaxParticles;  // queued large cells
-constexpr size_t kScratchBytes = kOffLarge + 8ull * (kMaxParticles / 64 + 2);
+constexpr size_t kOffScat = kOffLarge + align256(8ull * (kMaxParticles / 64 + 2));
+constexpr size_t kScratchBytes = kOffScat + 8ull * kMaxParticles;
 static_assert(sizeof(sphx::StepParams) + 16 <= 1024, "scene table fits its scratch slot");
 
 static __device__ __align__(256) uint4 g_scratch[kScratchBytes / sizeof(uint4)];
@@ -138,6 +139,7 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     B.key = reinterpret_cast<uint32_t *>(base + kOffKey);
     B.rank = reinterpret_cast<uint32_t *>(base + kOffRank);
     B.order = reinterpret_cast<uint32_t *>(base + kOffOrder);
+    B.scat = reinterpret_cast<uint2 *>(base + kOffScat);
     B.count = reinterpret_cast<uint32_t *>(base + kOffCount);
     B.start = reinterpret_cast<uint32_t *>(base + kOffStart);
     B.tile_sum = reinterpret_cast<uint32_t *>(base + kOffTiles);

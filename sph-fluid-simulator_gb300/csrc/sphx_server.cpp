@@ -45,7 +45,8 @@ struct Request {
 // sphx_api.cpp, with the grid estimated from the particle count.
 size_t footprint(uint32_t n) {
     // state, ids, records, sort scratch, staging, neighbour records and lists
-    const size_t per_particle = 16 * 4 + 4 * 2 + 16 + 16 + 4 * 3 + 24 + 32 + 4 * 64 + 4 + 1;
+    const size_t per_particle =
+        16 * 4 + 4 * 2 + 16 + 16 + 4 * 3 + 8 + 24 + 32 + 4 * sphx::kNbrSlotsDefault + 4 + 1;
     const size_t slots = 16ull * n + 4096;
     return per_particle * n + 8 * slots + 4096;
 }

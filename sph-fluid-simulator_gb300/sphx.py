@@ -57,7 +57,8 @@ class Options(C.Structure):
     _fields_ = [("reorder_interval", C.c_int), ("use_graph", C.c_int), ("device", C.c_int),
                 ("stream", C.c_void_p), ("grid_ymax", C.c_float), ("grid_dims", C.c_int * 3),
                 ("grid_origin", C.c_int * 3), ("max_cell_occupancy", C.c_uint32),
-                ("density_threads", C.c_int), ("force_threads", C.c_int)]
+                ("density_threads", C.c_int), ("force_threads", C.c_int),
+                ("neighbor_slots", C.c_uint32)]
 
 
 class SceneDesc(C.Structure):

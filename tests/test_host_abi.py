@@ -123,3 +123,13 @@ def test_reference_presets(sphx_lib):
     o = sphx_lib.default_options()
     assert o.reorder_interval == 1 and o.max_cell_occupancy == 16384
     assert o.density_threads == 256 and o.force_threads == 256
+    assert o.neighbor_slots == 256
+
+
+def test_neighbor_slots_bound(sphx_lib):
+    """A list longer than 1024 is refused before any device work."""
+    opt = sphx_lib.default_options(neighbor_slots=1025)
+    with pytest.raises(sphx_lib.SphxError) as e:
+        sphx_lib.Scene(sphx_lib.reference_settings(), sphx_lib.reference_box(),
+                       np.zeros((8, 3), np.float32), None, opt)
+    assert e.value.code == -1 and "neighbor_slots" in str(e.value)
