@@ -424,7 +424,7 @@ int sphx::run_steps(sphx_handle *h, float dt, int nsteps) {
             }
             cudaEvent_t *ev = &h->events[h->events_used];
             h->launches_per_step.resize(h->events.size() / 4);
-            h->launches_per_step[h->events_used / 4] = reorder ? 9u : 8u;
+            h->launches_per_step[h->events_used / 4] = reorder ? 10u : 9u;  // sort 7, gather, density, force
             h->events_used += 4;
             int pv = h->pv, idc = h->idc;
             SPHX_CUDA(enqueue_step(h, reorder, pv, idc, ev));
