@@ -33,6 +33,13 @@ METRIC = "particle-steps/s @2.1M"
 UNIT = "particle-steps/s"
 SIDE = 128  # 128^3 = 2,097,152 particles
 ALGO_BYTES = 80  # density 24 B + force 56 B per particle-step (compulsory FP32 SoA)
+# FP32 operations of the walk kernels: an r^2 test is 3 sub + 3 mul + 2 add;
+# an accepted pair costs the density 1 sub + 2 mul (cube) + 4 (compensated
+# add) and the force 41 (distance 8, rsqrt, r and h - r 2, two coefficients
+# 6, three components 3 x 4, compensated adds 12)
+OPS_PER_TEST = 8
+OPS_PER_PAIR_DENSITY = 7
+OPS_PER_PAIR_FORCE = 41
 WORKLOAD = ("dam-break block 128^3 = 2,097,152 particles, jittered cubic lattice spacing 0.05 m "
             "(+-5%), box 16 x 8 x 8 m (walls at bound +- h, floor y=0, no ceiling), h=0.1, "
             "rho0=1000, m=0.125, k=20, mu=1, g=-9.8, dt=0.002, damping 0.5")
@@ -371,6 +378,7 @@ def run_sphx(a):
     # warm-up, then the timed region with per-phase events recorded inside it
     sc.step(sphx.DT, a.warmup)
     sc.synchronize()
+    walk0 = sc.walk_stats()  # (r^2 tests, accepted pairs) of the window's first step
     sc.set_profiling(True)
     sc.kernel_times()  # reset accumulators
     e0 = torch.cuda.Event(enable_timing=True)
@@ -389,10 +397,14 @@ def run_sphx(a):
     kt = sc.kernel_times()
     value = n * a.steps * world / (ms / 1e3)
 
+    walk1 = sc.walk_stats()  # ... and of the state after its last step
     peak, peak_kind = peaks()
     dens_ms = kt.density_ms / max(kt.steps, 1)
     force_ms = kt.force_ms / max(kt.steps, 1)
     achieved = ALGO_BYTES * n / ((dens_ms + force_ms) / 1e3) / 1e9
+    tests = 0.5 * (walk0[0] + walk1[0])
+    pairs = 0.5 * (walk0[1] + walk1[1])
+    ops = tests * OPS_PER_TEST + pairs * (OPS_PER_PAIR_DENSITY + OPS_PER_PAIR_FORCE)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind,
                 "traffic": a.traffic if a.traffic is not None else profiled_traffic(n),
@@ -400,7 +412,15 @@ def run_sphx(a):
                                   "kernel (profiles/dram_traffic.json)",
                 "kernels": "k_density + k_force",
                 "per_step_ms": {"sort": kt.sort_ms / max(kt.steps, 1), "density": dens_ms,
-                                "force": force_ms}}
+                                "force": force_ms},
+                # the walk kernels are issue-bound, not bandwidth-bound: their work rates
+                "r2_tests_per_step": tests, "accepted_pairs_per_step": pairs,
+                "r2_tests_per_s": tests / (dens_ms / 1e3),
+                "fp32_ops_per_s": ops / ((dens_ms + force_ms) / 1e3),
+                "work_note": "mean of the window's first and last state (sphx_walk_stats); FP32 ops "
+                             "= %d per r^2 test + %d per accepted pair (density %d, force %d)"
+                             % (OPS_PER_TEST, OPS_PER_PAIR_DENSITY + OPS_PER_PAIR_FORCE,
+                                OPS_PER_PAIR_DENSITY, OPS_PER_PAIR_FORCE)}
     sc.set_profiling(False)
 
     # e2e through the C-ABI with pinned host buffers
@@ -456,7 +476,8 @@ def run_sphx(a):
     if world == 1 and a.batch_steps > 0:
         import sphx
         batched = batch_compare(sphx.batch_scenes(512, seed=0), a.batch_steps, 0, device)
-    ws_mb = n * (16 * 4 + 4 * 2 + 8 + 16 + 12) / 1e6
+    # state, ids, density, sort scratch, neighbour records and the list entries in use
+    ws_mb = (n * (16 * 4 + 4 * 2 + 16 + 12 + 8 + 32) + 4 * pairs) / 1e6
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
             "warmup": a.warmup, "ms_per_step": ms / a.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",

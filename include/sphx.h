@@ -206,6 +206,11 @@ int sphx_read_cells(sphx_handle *h, int32_t *cells3, uint16_t *hash16);
  * visits of the reference walk (src/sph.cpp:40-66) and the wrapping sum of
  * SplitMix64-finalised ids over them (a multiset fingerprint), id order. */
 int sphx_neighbor_digest(sphx_handle *h, uint32_t *count, uint64_t *digest);
+/* Work of one neighbour walk over the current positions, summed over all
+ * particles: candidates whose r^2 the step's walk evaluates, and accepted
+ * neighbour visits.  No counterpart in the reference (a diagnostic for the
+ * r^2-test and FP32 operation rates). */
+int sphx_walk_stats(sphx_handle *h, uint64_t *r2_tests, uint64_t *accepted);
 int sphx_device_state(sphx_handle *h, sphx_device_view *out);
 
 /* The reference's GPU seam, updateParticlesGPU(Particle*, glm::mat4*, size_t,

@@ -857,13 +857,44 @@ int sphx_neighbor_digest(sphx_handle *h, uint32_t *count, uint64_t *digest) {
     uint32_t *dcount = reinterpret_cast<uint32_t *>(h->staging);
     uint64_t *ddig = reinterpret_cast<uint64_t *>(h->staging + 2 * (size_t)h->cap_n);
     SPHX_CUDA(sphx::launch_sort(T, h->sb, h->pos[h->pv], h->stream));
-    SPHX_CUDA(sphx::launch_digest(T, h->sb, h->pos[h->pv], h->id[h->idc], dcount, ddig, true,
-                                  h->stream));
+    SPHX_CUDA(sphx::launch_digest(T, h->sb, h->pos[h->pv], h->id[h->idc], dcount, ddig, nullptr,
+                                  true, h->stream));
     rc = sphx::read_status(h);
     if (rc) return rc;
     SPHX_CUDA(cudaMemcpyAsync(count, dcount, 4 * n, cudaMemcpyDeviceToHost, h->stream));
     SPHX_CUDA(cudaMemcpyAsync(digest, ddig, 8 * n, cudaMemcpyDeviceToHost, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));
+    return SPHX_OK;
+}
+
+int sphx_walk_stats(sphx_handle *h, uint64_t *r2_tests, uint64_t *accepted) {
+    int rc = sphx_synchronize(h);
+    if (rc) return rc;
+    if (!r2_tests || !accepted) return fail(SPHX_ERR_INVALID, "null output");
+    rc = sphx::ensure_params(h, h->params_valid ? h->params_dt : 0.f);
+    if (rc) return rc;
+    const size_t n = h->n;
+    const sphx::SceneTable T = sphx::table_of(h);
+    // staging holds 24 bytes per particle: counts, tests, then 8-byte digests
+    uint32_t *dcount = reinterpret_cast<uint32_t *>(h->staging);
+    uint32_t *dtests = dcount + h->cap_n;
+    uint64_t *ddig = reinterpret_cast<uint64_t *>(h->staging + 2 * (size_t)h->cap_n);
+    SPHX_CUDA(sphx::launch_sort(T, h->sb, h->pos[h->pv], h->stream));
+    SPHX_CUDA(sphx::launch_digest(T, h->sb, h->pos[h->pv], h->id[h->idc], dcount, ddig, dtests,
+                                  true, h->stream));
+    rc = sphx::read_status(h);
+    if (rc) return rc;
+    std::vector<uint32_t> c(n), t(n);
+    SPHX_CUDA(cudaMemcpyAsync(c.data(), dcount, 4 * n, cudaMemcpyDeviceToHost, h->stream));
+    SPHX_CUDA(cudaMemcpyAsync(t.data(), dtests, 4 * n, cudaMemcpyDeviceToHost, h->stream));
+    SPHX_CUDA(cudaStreamSynchronize(h->stream));
+    uint64_t st = 0, sa = 0;
+    for (size_t k = 0; k < n; ++k) {
+        st += t[k];
+        sa += c[k];
+    }
+    *r2_tests = st;
+    *accepted = sa;
     return SPHX_OK;
 }
 

@@ -333,6 +333,7 @@ struct WalkCtx {
 template <class V>
 __device__ __forceinline__ void test_pair(const WalkCtx &W, uint32_t j, float4 pj, uint32_t self,
                                           float4 pi, uint32_t w, V &vis) {
+    vis.on_test();
     const float dx = __fsub_rn(pj.x, pi.x);
     const float dy = __fsub_rn(pj.y, pi.y);
     const float dz = __fsub_rn(pj.z, pi.z);
@@ -813,6 +814,7 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 // particle with more (clumped fluid) stores its count only and the force
 // kernel walks for it instead.
 struct DensityVisitor {
+    __device__ __forceinline__ void on_test() {}
     float h2;
     float acc, comp;  // compensated sum of (h^2 - r^2)^3
     uint32_t *row;    // &nbr[i * slots], or NULL: nothing recorded
@@ -921,9 +923,33 @@ __device__ __forceinline__ void pair_add_record(ForcePair &pair, float4 a, float
     pair.add(dx, dy, dz, d2, a.w, b);
 }
 
+// A neighbour's 32-byte record (32-byte aligned: fr is), read-only during
+// the force pass; one 256-bit load (four 64-bit lanes) where SPHX_REC256 is
+// set.
+#ifndef SPHX_REC256
+#define SPHX_REC256 1
+#endif
+__device__ __forceinline__ void load_record(const float4 *__restrict__ fr, uint32_t j, float4 &a,
+                                            float4 &b) {
+#if SPHX_REC256
+    const float4 *p = fr + 2 * (size_t)j;
+    unsigned long long q0, q1, q2, q3;
+    asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(q0), "=l"(q1), "=l"(q2), "=l"(q3) : "l"(p));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(q0));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a.z), "=f"(a.w) : "l"(q1));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(b.x), "=f"(b.y) : "l"(q2));
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(b.z), "=f"(b.w) : "l"(q3));
+#else
+    a = fr[2 * (size_t)j];
+    b = fr[2 * (size_t)j + 1];
+#endif
+}
+
 __device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *__restrict__ fr,
                                                  uint32_t j, float4 pi) {
-    pair_add_record(pair, fr[2 * (size_t)j], fr[2 * (size_t)j + 1], pi);
+    float4 a, b;
+    load_record(fr, j, a, b);
+    pair_add_record(pair, a, b, pi);
 }
 
 // Force walk over a chunk of neighbour records (RecordScan): a lane first
@@ -987,6 +1013,7 @@ struct RecordScan {
 
 // Lanes off the fast path add each accepted pair as the walk finds it.
 struct ForceVisitor {
+    __device__ __forceinline__ void on_test() {}
     ForcePair &pair;
     const float4 *__restrict__ fr;
     float4 pi;
@@ -1035,19 +1062,6 @@ __device__ __forceinline__ void integrate(const StepParams &P, float4 &x, float4
     }
 }
 
-// Force output, integration and the next state of particle i.
-__device__ __forceinline__ void force_finish(const StepParams &P, uint32_t i, float4 pi, float4 vi,
-                                             float rho, const ForcePair &pair,
-                                             float4 *__restrict__ pos_out,
-                                             float4 *__restrict__ vel_out,
-                                             float4 *__restrict__ force_out) {
-    const float fx = pair.fx, fy = pair.fy, fz = pair.fz;
-    force_out[i] = make_float4(fx, fy, fz, 0.f);
-    integrate(P, pi, vi, fx, fy, fz, rho);
-    pos_out[i] = pi;
-    vel_out[i] = vi;
-}
-
 // Force of every particle: over its list when its neighbours fit one (same
 // neighbours, same order as the density walk), else by a warp-cooperative
 // walk over the neighbour records in that same order.  Only the lanes past
@@ -1081,15 +1095,17 @@ __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads
             const uint32_t left = cnt - k;
             {  // two records in flight, then summed in list order
                 const uint32_t j1 = left > 1 ? e.y : e.x;
-                const float4 a0 = fr[2 * (size_t)e.x], b0 = fr[2 * (size_t)e.x + 1];
-                const float4 a1 = fr[2 * (size_t)j1], b1 = fr[2 * (size_t)j1 + 1];
+                float4 a0, b0, a1, b1;
+                load_record(fr, e.x, a0, b0);
+                load_record(fr, j1, a1, b1);
                 pair_add_record(pair, a0, b0, pi);
                 if (left > 1) pair_add_record(pair, a1, b1, pi);
             }
             if (left > 2) {
                 const uint32_t j3 = left > 3 ? e.w : e.z;
-                const float4 a2 = fr[2 * (size_t)e.z], b2 = fr[2 * (size_t)e.z + 1];
-                const float4 a3 = fr[2 * (size_t)j3], b3 = fr[2 * (size_t)j3 + 1];
+                float4 a2, b2, a3, b3;
+                load_record(fr, e.z, a2, b2);
+                load_record(fr, j3, a3, b3);
                 pair_add_record(pair, a2, b2, pi);
                 if (left > 3) pair_add_record(pair, a3, b3, pi);
             }
@@ -1126,6 +1142,8 @@ struct DigestVisitor {
     const uint32_t *__restrict__ id;
     uint32_t count;
     uint64_t sum;
+    uint32_t tests;  // candidates whose r^2 the walk evaluated
+    __device__ __forceinline__ void on_test() { ++tests; }
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float) {
         ++count;
         sum += mix64(id[j]);
@@ -1137,7 +1155,7 @@ constexpr int kDigestThreads = 256;
 template <bool kInd>
 __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ id,
                          uint32_t *__restrict__ count_out, uint64_t *__restrict__ digest_out,
-                         const uint32_t *__restrict__ status) {
+                         uint32_t *__restrict__ tests_out, const uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((t & ~31u) >= T.n || (status[0] & kStatusErrorMask)) return;
     const bool valid = t < T.n;
@@ -1148,7 +1166,7 @@ __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ i
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
-    DigestVisitor v{id, 0u, 0ull};
+    DigestVisitor v{id, 0u, 0ull, 0u};
     // the same walk as k_density's
     __shared__ PosSmem<kInd> s_coop[kDigestThreads / 32];
     PosScan<kInd, DigestVisitor> scan{s_coop[threadIdx.x >> 5], v};
@@ -1157,6 +1175,7 @@ __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ i
     const uint32_t d = T.pofs[sc] + id[i];
     count_out[d] = v.count;
     digest_out[d] = v.sum;
+    if (tests_out) tests_out[d] = v.tests;
 }
 
 // Rows [first, first + n) from host-ordered staging arrays (vel3 all zero
@@ -1428,14 +1447,16 @@ cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4
 }
 
 cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float4 *pos,
-                          const uint32_t *id, uint32_t *count, uint64_t *digest, bool indirect,
-                          cudaStream_t st) {
+                          const uint32_t *id, uint32_t *count, uint64_t *digest, uint32_t *tests,
+                          bool indirect, cudaStream_t st) {
     const WalkCtx G = global_ctx(B, pos);
     if (T.n) {
         if (indirect)
-            k_digest<true><<<blocks(T.n, kDigestThreads), kDigestThreads, 0, st>>>(T, G, id, count, digest, B.status);
+            k_digest<true><<<blocks(T.n, kDigestThreads), kDigestThreads, 0, st>>>(
+                T, G, id, count, digest, tests, B.status);
         else
-            k_digest<false><<<blocks(T.n, kDigestThreads), kDigestThreads, 0, st>>>(T, G, id, count, digest, B.status);
+            k_digest<false><<<blocks(T.n, kDigestThreads), kDigestThreads, 0, st>>>(
+                T, G, id, count, digest, tests, B.status);
     }
     return cudaGetLastError();
 }

@@ -68,9 +68,11 @@ cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4
                          const float4 *vel, const float4 *rp, const float4 *fr, const NbrList &L,
                          float4 *pos_out, float4 *vel_out, float4 *force_out, bool indirect,
                          cudaStream_t st, int threads = 256);
+// Per particle (scene offset + id): accepted neighbour visits, their id
+// fingerprint and, if tests is set, the candidates whose r^2 was evaluated.
 cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float4 *pos,
-                          const uint32_t *id, uint32_t *count, uint64_t *digest, bool indirect,
-                          cudaStream_t st);
+                          const uint32_t *id, uint32_t *count, uint64_t *digest, uint32_t *tests,
+                          bool indirect, cudaStream_t st);
 // Rows [first, first + n) from host-ordered staging (scene-local ids), and
 // back: one scene's rows to staging in its id order (field: 0 pos, 1 vel,
 // 2 force, 3 rho, 4 prs).

@@ -155,6 +155,7 @@ def lib():
         "sphx_read_transforms": (C.c_int, [vp, vp]),
         "sphx_read_cells": (C.c_int, [vp, vp, vp]),
         "sphx_neighbor_digest": (C.c_int, [vp, vp, vp]),
+        "sphx_walk_stats": (C.c_int, [vp, vp, vp]),
         "sphx_device_state": (C.c_int, [vp, P(DeviceView)]),
         "sphx_update_particles": (C.c_int, [vp, vp, C.c_size_t, P(Settings), P(Box), C.c_float]),
         "sphx_update_particles_release": (C.c_int, []),
@@ -493,6 +494,14 @@ class Scene:
         dig = np.zeros(self.n, np.uint64)
         _check(lib().sphx_neighbor_digest(self.h, _ptr(cnt), _ptr(dig)))
         return cnt, dig
+
+    def walk_stats(self):
+        """(candidates whose r^2 the walk evaluates, accepted neighbour visits)
+        for the current positions, summed over all particles."""
+        t = C.c_uint64()
+        a = C.c_uint64()
+        _check(lib().sphx_walk_stats(self.h, C.byref(t), C.byref(a)))
+        return t.value, a.value
 
     def device_view(self):
         v = DeviceView()

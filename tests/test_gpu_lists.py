@@ -60,3 +60,16 @@ def test_walking_force_matches_oracle(sphx_lib, port):
     print("force: gpu-vs-f64 %.2e  ref-vs-f64 %.2e  gpu-vs-ref %.2e"
           % (e_gpu, e_ref, rel_err(out["force"], r.force)))
     assert e_gpu < REL_TOL and e_gpu <= max(2 * e_ref, 1e-6)
+
+
+def test_walk_stats_agree_with_digest(sphx_lib):
+    """sphx_walk_stats counts what the walk does: its accepted visits are the
+    digest's counts, every accepted pair was an r^2 test, and a uniform
+    lattice spends a bounded number of tests per accepted pair."""
+    pos, box = sphx_lib.dambreak(24, box_dims=(2.0, 2.0, 2.0), seed=5)
+    s = sphx_lib.Settings(*[float(x) for x in CONFIG_ARGS])
+    with sphx_lib.Scene(s, box, pos) as sc:
+        tests, acc = sc.walk_stats()
+        cnt, _ = sc.neighbor_digest()
+    assert acc == int(cnt.sum())
+    assert acc <= tests <= 8 * acc
