@@ -65,8 +65,8 @@ typedef struct sphx_options {
     int grid_dims[3];      /* cell-grid dimensions; 0: automatic (each >= 5) */
     int grid_origin[3];    /* cell coordinates of grid slot 0 (used when grid_dims set) */
     uint32_t max_cell_occupancy; /* particles per cell before a step fails (0 or > 16384: 16384) */
-    int density_threads;   /* block size of the density kernel: 128 or 256 (0: 256) */
-    int force_threads;     /* block size of the force kernel: 128 or 256 (0: 256) */
+    int density_threads;   /* block size of the density kernel: 128 or 256 (0: 128) */
+    int force_threads;     /* block size of the force kernel: 128 or 256 (0: 128) */
     uint32_t neighbor_slots; /* accepted neighbours the density pass records per particle for
                                 the force pass (0: 256, at most 1024); particles with more are
                                 walked again by the force pass */
@@ -186,7 +186,9 @@ int sphx_scene_range(const sphx_handle *h, size_t scene, size_t *first, size_t *
 int sphx_read_scene(sphx_handle *h, size_t scene, float *pos3, float *vel3, float *rho,
                     float *prs, float *force3);
 /* Replaces positions / velocities (host, id order, vel3 may be NULL) and
- * clears an error state. */
+ * clears an error state.  A non-finite position, or one whose cell quotient
+ * x / h reaches 2^30, returns SPHX_ERR_DOMAIN and leaves the handle in the
+ * error state until a valid replacement. */
 int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3);
 /* Enqueues nsteps steps of dt (asynchronous; errors raised by the kernels
  * surface at the next sphx_synchronize or read). */

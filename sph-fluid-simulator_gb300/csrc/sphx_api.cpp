@@ -228,14 +228,14 @@ int upload_tables(sphx_handle *h) {
 // Uploads one scene's host state into rows [first, first + n) of buffer
 // parity (pv, idc), with scene-local ids.
 int upload_scene(sphx_handle *h, const sphx::Scene &sc, const float *pos3, const float *vel3,
-                 int pv, int idc) {
+                 int pv, int idc, uint32_t *bad = nullptr) {
     const size_t n = sc.n;
     float *sp = h->staging, *sv = h->staging + 3 * (size_t)h->cap_n;
     SPHX_CUDA(cudaMemcpyAsync(sp, pos3, 12 * n, cudaMemcpyHostToDevice, h->stream));
     if (vel3) SPHX_CUDA(cudaMemcpyAsync(sv, vel3, 12 * n, cudaMemcpyHostToDevice, h->stream));
     else SPHX_CUDA(cudaMemsetAsync(sv, 0, 12 * n, h->stream));
     SPHX_CUDA(sphx::launch_upload_rows(sc.first, sc.n, sp, sv, h->pos[pv], h->vel[pv], h->id[idc],
-                                       h->stream));
+                                       sc.d.h, bad, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));  // staging is reused by the next scene
     return SPHX_OK;
 }
@@ -361,7 +361,7 @@ int run_graph_step(sphx_handle *h, bool reorder) {
     return SPHX_OK;
 }
 
-int normalise_threads(int t) { return t == 128 ? 128 : 256; }
+int normalise_threads(int t) { return t == 256 ? 256 : 128; }
 
 #define HANDLE_CHECK(h)                                                 \
     do {                                                                \
@@ -744,20 +744,30 @@ int sphx_scene_range(const sphx_handle *h, size_t scene, size_t *first, size_t *
 int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3) {
     HANDLE_CHECK(h);
     if (!pos3) return fail(SPHX_ERR_INVALID, "null positions");
-    for (const sphx::Scene &sc : h->scenes) {
-        const int rc = check_positions(pos3 + 3ull * sc.first, sc.n, sc.s.h);
-        if (rc) return rc;
-    }
-    SPHX_CUDA(cudaStreamSynchronize(h->stream));
+    // the domain check runs in the upload kernel: status word 3 ends as the
+    // first offending row, or stays all ones
+    uint32_t *bad = h->sb.status + 3;
+    SPHX_CUDA(cudaMemsetAsync(bad, 0xFF, 4, h->stream));
     for (const sphx::Scene &sc : h->scenes) {
         const int rc = upload_scene(h, sc, pos3 + 3ull * sc.first,
-                                    vel3 ? vel3 + 3ull * sc.first : nullptr, h->pv, h->idc);
+                                    vel3 ? vel3 + 3ull * sc.first : nullptr, h->pv, h->idc, bad);
         if (rc) return rc;
     }
     SPHX_CUDA(cudaMemsetAsync(h->sb.status, 0, 8, h->stream));
     SPHX_CUDA(cudaMemsetAsync(h->rp, 0, 16ull * h->n, h->stream));
     SPHX_CUDA(cudaMemsetAsync(h->force, 0, 16ull * h->n, h->stream));
+    SPHX_CUDA(cudaMemcpyAsync(h->h_status, bad, 4, cudaMemcpyDeviceToHost, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));
+    const uint32_t row = *h->h_status;
+    if (row != 0xffffffffu) {
+        // the state now holds the rejected positions: refuse to step on it
+        h->error = SPHX_ERR_DOMAIN;
+        size_t k = 0;
+        while (k + 1 < h->scenes.size() && row >= h->scenes[k + 1].first) ++k;
+        return fail(SPHX_ERR_DOMAIN, "scene " + std::to_string(k) + " position " +
+                                         std::to_string(row - h->scenes[k].first) +
+                                         " is non-finite or too far from the origin");
+    }
     h->error = 0;
     return SPHX_OK;
 }

@@ -74,8 +74,8 @@ void sphx_options_default(sphx_options *o) {
     o->stream = nullptr;
     o->grid_ymax = 0.f;
     o->max_cell_occupancy = 16384;
-    o->density_threads = 256;
-    o->force_threads = 256;
+    o->density_threads = 128;
+    o->force_threads = 128;
     o->neighbor_slots = 256;
 }
 

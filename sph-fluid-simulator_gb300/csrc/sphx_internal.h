@@ -28,8 +28,8 @@ Derived derive_constants(float mass, float restDensity, float gasConst, float vi
 
 // Block sizes of the two walk kernels and the reorder interval.
 struct Tuning {
-    int density_threads = 256;
-    int force_threads = 256;
+    int density_threads = 128;
+    int force_threads = 128;
     int reorder_interval = 1;
 };
 

@@ -1180,13 +1180,23 @@ __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ i
 
 // Rows [first, first + n) from host-ordered staging arrays (vel3 all zero
 // or uploaded); ids are scene-local: row - first.
+// With `bad` set, a position that is non-finite or whose cell quotient x / h
+// is 2^30 or more in magnitude (the host check of a new scene, done here for
+// state replacements) lowers *bad to its row.
 __global__ void k_upload_rows(uint32_t first, uint32_t n, const float *__restrict__ pos3,
                               const float *__restrict__ vel3, float4 *__restrict__ pos,
-                              float4 *__restrict__ vel, uint32_t *__restrict__ id) {
+                              float4 *__restrict__ vel, uint32_t *__restrict__ id, float h,
+                              uint32_t *__restrict__ bad) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t r = first + i;
-    pos[r] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], 0.f);
+    const float x = pos3[3 * i], y = pos3[3 * i + 1], z = pos3[3 * i + 2];
+    if (bad) {
+        const bool ok = in_domain(__fdiv_rn(x, h)) && in_domain(__fdiv_rn(y, h)) &&
+                        in_domain(__fdiv_rn(z, h));  // NaN and inf fail the bound too
+        if (!ok) atomicMin(bad, r);
+    }
+    pos[r] = make_float4(x, y, z, 0.f);
     vel[r] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.f);
     id[r] = i;
 }
@@ -1462,8 +1472,9 @@ cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float
 }
 
 cudaError_t launch_upload_rows(uint32_t first, uint32_t n, const float *pos3, const float *vel3,
-                               float4 *pos, float4 *vel, uint32_t *id, cudaStream_t st) {
-    if (n) k_upload_rows<<<blocks(n, 256), 256, 0, st>>>(first, n, pos3, vel3, pos, vel, id);
+                               float4 *pos, float4 *vel, uint32_t *id, float h, uint32_t *bad,
+                               cudaStream_t st) {
+    if (n) k_upload_rows<<<blocks(n, 256), 256, 0, st>>>(first, n, pos3, vel3, pos, vel, id, h, bad);
     return cudaGetLastError();
 }
 

@@ -429,7 +429,7 @@ class Scene:
         _check(lib().sphx_get_tuning(self.h, C.byref(t)))
         return t
 
-    def set_tuning(self, density_threads=256, force_threads=256, reorder_interval=1):
+    def set_tuning(self, density_threads=128, force_threads=128, reorder_interval=1):
         t = Tuning(density_threads, force_threads, reorder_interval, 0.0)
         _check(lib().sphx_set_tuning(self.h, C.byref(t)))
 

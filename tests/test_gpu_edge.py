@@ -120,3 +120,29 @@ def test_rollout_100_steps_statistics(sphx_lib, port):
     print("100-step drift: mean density %.2e, kinetic energy %.2e, centre of mass %.2e m"
           % (e_rho, e_ke, e_com))
     assert e_rho < 5e-3 and e_ke < 5e-2 and e_com < 5e-3
+
+
+def test_set_state_rejects_out_of_domain(sphx_lib):
+    """State replacement is validated on the device: the first bad row is
+    named, stepping is refused until a valid state replaces it."""
+    sphx = sphx_lib
+    pos, box = sphx.dambreak(6, box_dims=(1, 1, 1))
+    with scene(sphx, pos, box=box) as sc:
+        sc.step(0.002, 1)
+        bad = pos.copy()
+        bad[17, 2] = np.inf
+        bad[40, 0] = np.nan
+        with pytest.raises(sphx.SphxError) as e:
+            sc.set_state(bad)
+        assert e.value.code == -4 and "position 17" in str(e.value)
+        with pytest.raises(sphx.SphxError) as e:
+            sc.step(0.002, 1)
+        assert e.value.code == -6
+        far = pos.copy()
+        far[3, 1] = 0.1 * 2.0 ** 31  # cell quotient past 2^30
+        with pytest.raises(sphx.SphxError) as e:
+            sc.set_state(far)
+        assert e.value.code == -4 and "position 3" in str(e.value)
+        sc.set_state(pos)
+        sc.step(0.002, 2)
+        sc.synchronize()

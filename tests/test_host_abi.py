@@ -122,7 +122,7 @@ def test_reference_presets(sphx_lib):
     assert np.float32(b.damping) == np.float32(0.5) and np.float32(b.offset) == np.float32(1e-4)
     o = sphx_lib.default_options()
     assert o.reorder_interval == 1 and o.max_cell_occupancy == 16384
-    assert o.density_threads == 256 and o.force_threads == 256
+    assert o.density_threads == 128 and o.force_threads == 128
     assert o.neighbor_slots == 256
 
 
