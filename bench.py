@@ -207,8 +207,7 @@ def run_batch(a):
     torch.cuda.set_device(local)
     scenes = sphx.batch_scenes(512, seed=0)
     res = batch_compare(scenes, a.steps, a.warmup, local,
-                        cache_path=os.path.join(ROOT, "gpurun_out", "autotune.txt")
-                        if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None)
+                        cache_path=os.environ.get("SPHX_TUNE_CACHE"))
     line = {"metric": "scenes/s (512 scenes, batched vs one at a time)", "value": res["batched_scenes_per_s"],
             "unit": "scenes/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
