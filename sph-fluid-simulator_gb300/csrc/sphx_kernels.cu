@@ -589,6 +589,14 @@ __device__ __forceinline__ void walk(const WalkCtx &W, const WalkStart &s, uint3
 #ifndef SPHX_COOP_SEARCH
 #define SPHX_COOP_SEARCH 1
 #endif
+// Rows and x windows narrowed by each particle's y, z gaps to the rows
+#ifndef SPHX_COOP_NARROW
+#define SPHX_COOP_NARROW 1
+#endif
+#ifndef SPHX_SCAN_UNROLL
+#define SPHX_SCAN_UNROLL 4
+#endif
+constexpr int kScanUnroll = SPHX_SCAN_UNROLL;
 
 constexpr uint32_t kCoopChunk = SPHX_COOP_CHUNK;
 
@@ -615,8 +623,12 @@ template <bool kInd, class S>
 __device__ __forceinline__ void coop_rows_group(const WalkCtx &W, const WalkStart &s, uint32_t self,
                                                 float4 pi, uint32_t gmask, uint32_t lane, S &scan) {
     const float h = W.h;
+#if SPHX_COOP_NARROW
     const float eym = gap_to_cell(pi.y, s.c.cy, -1, h), eyp = gap_to_cell(pi.y, s.c.cy, 1, h);
     const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
+#else
+    const float eym = 0.f, eyp = 0.f, ezm = 0.f, ezp = 0.f;
+#endif
     const float ey2[3] = {eym * eym, 0.f, eyp * eyp};
     const float ez2[3] = {ezm * ezm, 0.f, ezp * ezp};
     uint32_t rows = 0;
@@ -785,12 +797,15 @@ struct PosScan {
             lo = l;
         }
 #endif
-        uint32_t k = lo;
-#pragma unroll 2
-        for (; k < hi; ++k) {
+        // every candidate from the searched start on has x >= xlo
+#pragma unroll kScanUnroll
+        for (uint32_t k = lo; k < hi; ++k) {
             const float4 p = sm.p(k);
             if (p.x > xhi) return true;
-            if (p.x >= xlo) test_pair(W, kInd ? sm.idx[k] : c0 + k, p, self, pi, 1u, vis);
+#if !SPHX_COOP_SEARCH
+            if (p.x < xlo) continue;
+#endif
+            test_pair(W, kInd ? sm.idx[k] : c0 + k, p, self, pi, 1u, vis);
         }
         return false;
     }
