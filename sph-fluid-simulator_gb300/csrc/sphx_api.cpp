@@ -613,13 +613,21 @@ int sphx::read_scene(sphx_handle *h, size_t k, float *pos3, float *vel3, float *
                   {force3, 2, h->force, 3ull * sc.n},
                   {rho, 3, nullptr, sc.n},
                   {prs, 4, nullptr, sc.n}};
+    const size_t cap = 6ull * h->cap_n;
+    size_t used = 0;
     for (const F &f : fields) {
         if (!f.dst) continue;
-        SPHX_CUDA(sphx::launch_read_rows(sc.first, sc.n, f.field, h->id[h->idc], f.src, h->rp,
-                                         h->staging, h->stream));
-        SPHX_CUDA(cudaMemcpyAsync(f.dst, h->staging, 4 * f.floats, cudaMemcpyDeviceToHost, h->stream));
-        SPHX_CUDA(cudaStreamSynchronize(h->stream));
+        if (used + f.floats > cap) {
+            SPHX_CUDA(cudaStreamSynchronize(h->stream));
+            used = 0;
+        }
+        float *out = h->staging + used;
+        SPHX_CUDA(sphx::launch_read_rows(sc.first, sc.n, f.field, h->id[h->idc], f.src, h->rp, out,
+                                         h->stream));
+        SPHX_CUDA(cudaMemcpyAsync(f.dst, out, 4 * f.floats, cudaMemcpyDeviceToHost, h->stream));
+        used += f.floats;
     }
+    SPHX_CUDA(cudaStreamSynchronize(h->stream));
     return SPHX_OK;
 }
 
@@ -802,14 +810,22 @@ int sphx_read_state(sphx_handle *h, float *pos3, float *vel3, float *rho, float 
                   {force3, 2, h->force, 3 * n},
                   {rho, 3, nullptr, n},
                   {prs, 4, nullptr, n}};
+    // fields share the staging area (6 floats per particle of capacity) and
+    // wait only when it is full
+    const size_t cap = 6ull * h->cap_n;
+    size_t used = 0;
     for (const F &f : fields) {
         if (!f.dst) continue;
-        SPHX_CUDA(sphx::launch_read_field(T, f.field, h->id[h->idc], f.src, h->rp, h->staging,
-                                          h->stream));
-        SPHX_CUDA(cudaMemcpyAsync(f.dst, h->staging, 4 * f.floats, cudaMemcpyDeviceToHost,
-                                  h->stream));
-        SPHX_CUDA(cudaStreamSynchronize(h->stream));
+        if (used + f.floats > cap) {
+            SPHX_CUDA(cudaStreamSynchronize(h->stream));
+            used = 0;
+        }
+        float *out = h->staging + used;
+        SPHX_CUDA(sphx::launch_read_field(T, f.field, h->id[h->idc], f.src, h->rp, out, h->stream));
+        SPHX_CUDA(cudaMemcpyAsync(f.dst, out, 4 * f.floats, cudaMemcpyDeviceToHost, h->stream));
+        used += f.floats;
     }
+    SPHX_CUDA(cudaStreamSynchronize(h->stream));
     return SPHX_OK;
 }
 
