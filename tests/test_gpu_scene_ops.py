@@ -85,4 +85,3 @@ def test_settings_change_matches_fresh_scene(sphx_lib):
         ref = fresh.read()
     for f in ("pos", "vel", "rho", "prs", "force"):
         assert rel_err(got[f], ref[f]) < REL_TOL, f
-
