@@ -369,7 +369,7 @@ __device__ __forceinline__ void scan_run(const WalkCtx &W, uint32_t a, uint32_t 
 // is not monotone in x and candidates past xhi are skipped, not the rest of
 // the run.
 #ifndef SPHX_WINDOW_SEARCH
-#define SPHX_WINDOW_SEARCH 0
+#define SPHX_WINDOW_SEARCH 1
 #endif
 
 template <bool kInd, class V>
@@ -450,12 +450,8 @@ __device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, in
     const Grid &g = W.grid;
     if (mx >= 1 && mx + 1 < g.gx) {
         const float h = W.h;
-#if SPHX_NO_YZ_NARROW
-        const float eym = 0.f, eyp = 0.f, ezm = 0.f, ezp = 0.f;
-#else
         const float eym = gap_to_cell(pi.y, c.cy, -1, h), eyp = gap_to_cell(pi.y, c.cy, 1, h);
         const float ezm = gap_to_cell(pi.z, c.cz, -1, h), ezp = gap_to_cell(pi.z, c.cz, 1, h);
-#endif
         const float ey2[3] = {eym * eym, 0.f, eyp * eyp};
         const float ez2[3] = {ezm * ezm, 0.f, ezp * ezp};
         uint32_t rows = 0;
@@ -589,10 +585,6 @@ __device__ __forceinline__ void walk(const WalkCtx &W, const WalkStart &s, uint3
 #ifndef SPHX_COOP_SEARCH
 #define SPHX_COOP_SEARCH 1
 #endif
-// Rows and x windows narrowed by each particle's y, z gaps to the rows
-#ifndef SPHX_COOP_NARROW
-#define SPHX_COOP_NARROW 1
-#endif
 #ifndef SPHX_SCAN_UNROLL
 #define SPHX_SCAN_UNROLL 4
 #endif
@@ -623,12 +615,8 @@ template <bool kInd, class S>
 __device__ __forceinline__ void coop_rows_group(const WalkCtx &W, const WalkStart &s, uint32_t self,
                                                 float4 pi, uint32_t gmask, uint32_t lane, S &scan) {
     const float h = W.h;
-#if SPHX_COOP_NARROW
     const float eym = gap_to_cell(pi.y, s.c.cy, -1, h), eyp = gap_to_cell(pi.y, s.c.cy, 1, h);
     const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
-#else
-    const float eym = 0.f, eyp = 0.f, ezm = 0.f, ezp = 0.f;
-#endif
     const float ey2[3] = {eym * eym, 0.f, eyp * eyp};
     const float ez2[3] = {ezm * ezm, 0.f, ezp * ezp};
     uint32_t rows = 0;
