@@ -4,9 +4,11 @@
 //   k_keys        cell of every particle -> slot key in a modular cell grid,
 //                 per-slot counts (atomics) and each particle's arrival rank
 //   k_scan_*      exclusive prefix sum of the counts -> cellStart[slot]
-//   k_scatter     order[cellStart[key] + rank] = particle
-//   k_cellsort    within each cell run, ascending particle index, so that the
-//                 order (and hence every float sum) is deterministic
+//   k_scatter     (particle, x) into its cell's run, in arrival order
+//   k_cellsort    each particle's place in its cell's run by (x, index), so
+//                 that rows of cells are x-sorted and the order (and hence
+//                 every float sum) is deterministic (k_cellsort_large: cells
+//                 of more than 64 particles)
 //   k_gather      every R steps: permute pos/vel/id into cell order
 //   k_density     poly6 density and pressure            (sph.cpp:28-76)
 //   k_force       spiky pressure + viscosity force, then integration and
