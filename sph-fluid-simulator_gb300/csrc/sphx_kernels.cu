@@ -852,6 +852,13 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
 #ifndef SPHX_DENSITY_COOP
 #define SPHX_DENSITY_COOP 1
 #endif
+// No list is recorded for a particle whose cell holds more than
+// slots / kListSkipFactor particles; its count then carries kNoList.
+#ifndef SPHX_LIST_SKIP_FACTOR
+#define SPHX_LIST_SKIP_FACTOR 4
+#endif
+constexpr uint32_t kListSkipFactor = SPHX_LIST_SKIP_FACTOR;
+constexpr uint32_t kNoList = 0x80000000u;
 
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThreads)
@@ -868,8 +875,17 @@ __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThrea
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
-    DensityVisitor v{P.h2, 0.f, 0.f, valid && L.nbr ? L.nbr + (size_t)i * L.slots : nullptr, L.slots,
-                     0u};
+    uint32_t *row = nullptr;
+    if (valid && L.nbr) {
+        // A particle of a crowded cell (clumped fluid) has more neighbours
+        // than its list holds, and the force pass walks for it: recording
+        // them would only cost writes.  Either way the force is the same.
+        const uint32_t k = ((uint32_t)s.mz * (uint32_t)W.grid.gy + (uint32_t)s.my) *
+                               (uint32_t)W.grid.gx + (uint32_t)s.mx;
+        const uint32_t occ = W.start[k + 1] - W.start[k];
+        if (occ * kListSkipFactor <= L.slots) row = L.nbr + (size_t)i * L.slots;
+    }
+    DensityVisitor v{P.h2, 0.f, 0.f, row, L.slots, 0u};
 #if SPHX_DENSITY_COOP
     __shared__ PosSmem<kInd> s_coop[kThreads / 32];
     PosScan<kInd, DensityVisitor> scan{s_coop[threadIdx.x >> 5], v};
@@ -882,7 +898,7 @@ __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThrea
     const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
     const float inv = __frcp_rn(rho);
     rp[i] = make_float4(rho, prs, inv, 0.f);
-    if (L.nbr) L.count[i] = v.cnt;
+    if (L.nbr) L.count[i] = row ? v.cnt : (v.cnt | kNoList);
     if (fr) {
         // what the force kernel reads of a neighbour, in one 32-byte record
         const float4 vi = vel[i];
