@@ -816,8 +816,8 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
 // Accepted neighbours of a particle, in walk order, are also recorded for
 // the force kernel: entry k of particle i is nbr[i * slots + k], k < slots
 // (one contiguous row per particle, written by one lane front to back); a
-// particle with more (clumped fluid) stores its count only and the force
-// kernel walks for it instead.
+// particle with more (clumped fluid), or of a crowded cell, stores its count
+// only and the force kernel walks for it instead.
 struct DensityVisitor {
     __device__ __forceinline__ void on_test() {}
     float h2;
@@ -833,9 +833,6 @@ struct DensityVisitor {
     }
 };
 
-// sph.cpp:28-76.  The reference accumulates m*poly6*(h^2-r^2)^3 term by term;
-// here the cubes are summed and scaled once (the two differ by float
-// rounding only).
 // Per-thread walk context of scene sc.
 __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &G, uint32_t sc,
                                             const StepParams &P, const uint32_t *status) {
@@ -860,6 +857,9 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
 constexpr uint32_t kListSkipFactor = SPHX_LIST_SKIP_FACTOR;
 constexpr uint32_t kNoList = 0x80000000u;
 
+// Density and pressure, sph.cpp:28-76.  The reference accumulates
+// m*poly6*(h^2-r^2)^3 term by term; here the cubes are summed (compensated)
+// and scaled once: the two differ by float rounding only.
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
