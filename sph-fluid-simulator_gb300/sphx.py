@@ -17,7 +17,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libsphx.so")
+# SPHX_LIB names another build of the library (a tuning variant)
+LIB_PATH = os.environ.get("SPHX_LIB") or os.path.join(HERE, "lib", "libsphx.so")
 
 SPHX_OK = 0
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "NOMEM", -4: "DOMAIN", -5: "OVERFLOW", -6: "STATE"}
