@@ -64,11 +64,27 @@ sphx::Grid choose_grid(const sphx_box &b, const sphx_options &o, float h, const 
                        size_t n) {
     float lo[3] = {b.xmin, b.ymin, b.zmin}, hi[3] = {b.xmax, b.ymin, b.zmax};
     float plo[3] = {INFINITY, INFINITY, INFINITY}, phi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (size_t i = 0; i < n; ++i)
-        for (int a = 0; a < 3; ++a) {
-            plo[a] = std::min(plo[a], pos3[3 * i + a]);
-            phi[a] = std::max(phi[a], pos3[3 * i + a]);
+    // four particles (12 floats) per iteration, one accumulator per float:
+    // the inner loop vectorises; accumulator k holds component k % 3
+    float blo[12], bhi[12];
+    for (int k = 0; k < 12; ++k) {
+        blo[k] = INFINITY;
+        bhi[k] = -INFINITY;
+    }
+    const size_t m = 3 * n, m12 = m - m % 12;
+    for (size_t i = 0; i < m12; i += 12)
+        for (int k = 0; k < 12; ++k) {
+            blo[k] = std::min(blo[k], pos3[i + k]);
+            bhi[k] = std::max(bhi[k], pos3[i + k]);
         }
+    for (int k = 0; k < 12; ++k) {
+        plo[k % 3] = std::min(plo[k % 3], blo[k]);
+        phi[k % 3] = std::max(phi[k % 3], bhi[k]);
+    }
+    for (size_t i = m12; i < m; ++i) {
+        plo[i % 3] = std::min(plo[i % 3], pos3[i]);
+        phi[i % 3] = std::max(phi[i % 3], pos3[i]);
+    }
     for (int a = 0; a < 3; ++a) {
         lo[a] = std::min(lo[a], plo[a]);
         hi[a] = std::max(hi[a], phi[a]);
