@@ -107,6 +107,11 @@ def integrate_np(pos, vel, force, rho, args, box, dt):
     m = x[:, 1] < ylo
     x[m, 1] = (-x[m, 1] + f32(2) * ylo) + off
     v[m, 1] = -v[m, 1] * damp
+    if box.has_ceiling:  # the optional ceiling, after the floor
+        yhi = f32(box.ymax) - h
+        m = x[:, 1] > yhi
+        x[m, 1] = (-x[m, 1] + f32(2) * yhi) - off
+        v[m, 1] = -v[m, 1] * damp
     for ax, lo, hi in ((0, xlo, xhi), (2, zlo, zhi)):
         m = x[:, ax] < lo
         x[m, ax] = (-x[m, ax] + f32(2) * lo) + off
@@ -128,6 +133,28 @@ def test_integration_and_walls_bit_exact(sphx_lib):
     assert np.array_equal(bits(out["pos"]), bits(x))
     assert np.array_equal(bits(out["vel"]), bits(v))
     assert (x[:, 0] > box.xmin).all()
+
+
+def test_ceiling_bit_exact(sphx_lib, port):
+    """The optional ceiling (not in the reference's box) reflects like the
+    floor; integration stays bit-exact, and the step matches the oracle's
+    with the same ceiling."""
+    pos, box = sphx_lib.dambreak(12, box_dims=(1.2, 1.0, 1.2))
+    pos[:, 1] += np.float32(0.3)            # the block's top near the ceiling
+    box.ymax, box.has_ceiling = 1.0, 1
+    vel = np.random.default_rng(7).normal(0, 3.0, pos.shape).astype(np.float32)
+    vel[:, 1] = np.abs(vel[:, 1])           # upwards
+    with scene(sphx_lib, CONFIG_ARGS, pos, vel, box=box) as sc:
+        sc.step(0.002, 1)
+        out = sc.read()
+    x, v = integrate_np(pos, vel, out["force"], out["rho"], CONFIG_ARGS, box, 0.002)
+    assert np.array_equal(bits(out["pos"]), bits(x))
+    assert np.array_equal(bits(out["vel"]), bits(v))
+    assert (out["pos"][:, 1] <= np.float32(0.9) + np.float32(1e-3)).all()
+    assert (out["vel"][:, 1] < 0).sum() > 0  # some bounced
+    r = port.step(pos, vel, CONFIG_ARGS, 0.002, box=box.as_array()).by_id()
+    for f in ("rho", "prs", "force", "pos", "vel"):
+        assert rel_err(out[f], getattr(r, f)) < REL_TOL, f
 
 
 def test_transforms_match_reference(sphx_lib, golden):
@@ -200,6 +227,21 @@ def test_dense_collision_region_digest(sphx_lib, port):
         cnt, dig = sc.neighbor_digest()
     c2, d2 = port.neighbor_digest(pos, 0.1)
     assert np.array_equal(cnt, c2) and np.array_equal(dig, d2)
+
+
+def test_exact_lattice_on_cell_faces_digest(sphx_lib, port):
+    """An unjittered lattice at spacing h/2 around the origin puts particles
+    on (or a rounding away from) cell faces, across the double-width cell 0
+    and the bucket-collision region: accepted multisets bit-exact, through
+    the direct-addressed walk of a reordering step."""
+    k = np.arange(-15, 16, dtype=np.float32) * np.float32(0.05)
+    g = np.stack(np.meshgrid(k, k + np.float32(0.8), k, indexing="ij"), -1).reshape(-1, 3)
+    pos = np.ascontiguousarray(g, dtype=np.float32)
+    with scene(sphx_lib, CONFIG_ARGS, pos) as sc:
+        cnt, dig = sc.neighbor_digest()
+    c2, d2 = port.neighbor_digest(pos, 0.1)
+    assert np.array_equal(cnt, c2) and np.array_equal(dig, d2)
+    assert cnt.max() > 0
 
 
 @pytest.mark.parametrize("R", [1, 4, 16])
