@@ -905,9 +905,16 @@ int sphx_neighbor_digest(sphx_handle *h, uint32_t *count, uint64_t *digest) {
     const sphx::SceneTable T = sphx::table_of(h);
     uint32_t *dcount = reinterpret_cast<uint32_t *>(h->staging);
     uint64_t *ddig = reinterpret_cast<uint64_t *>(h->staging + 2 * (size_t)h->cap_n);
-    SPHX_CUDA(sphx::launch_sort(T, h->sb, h->pos[h->pv], h->stream));
-    SPHX_CUDA(sphx::launch_digest(T, h->sb, h->pos[h->pv], h->id[h->idc], dcount, ddig, nullptr,
-                                  true, h->stream));
+    // The walk of a reordering step: the state moved into cell order (into
+    // the other half of the ping-pong buffers, free between steps), walked
+    // with direct addressing.  (sphx_walk_stats walks through the
+    // permutation instead, as the steps between reorders do.)
+    const int pv = h->pv, idc = h->idc;
+    SPHX_CUDA(sphx::launch_sort(T, h->sb, h->pos[pv], h->stream));
+    SPHX_CUDA(sphx::launch_gather(T.n, h->sb, h->pos[pv], h->vel[pv], h->id[idc], h->pos[pv ^ 1],
+                                  h->vel[pv ^ 1], h->id[idc ^ 1], h->stream));
+    SPHX_CUDA(sphx::launch_digest(T, h->sb, h->pos[pv ^ 1], h->id[idc ^ 1], dcount, ddig, nullptr,
+                                  false, h->stream));
     rc = sphx::read_status(h);
     if (rc) return rc;
     SPHX_CUDA(cudaMemcpyAsync(count, dcount, 4 * n, cudaMemcpyDeviceToHost, h->stream));
