@@ -157,7 +157,7 @@ struct Layout {
     enum {
         kPos0, kPos1, kVel0, kVel1, kId0, kId1, kRp, kForce, kKey, kRank, kOrder, kCount,
         kStart, kTiles, kStatus, kStaging, kParams, kPofs, kSofs, kLarge, kFr, kNbr, kNcount,
-        kScat, kNum
+        kScat, kRofs, kRowOfs, kNum
     };
     size_t off[kNum];
     size_t total;
@@ -170,7 +170,8 @@ Layout layout_for(size_t cn, size_t cs, size_t csc, size_t slots) {
                                         4 * (cs + 1), 4 * (cs + 1), 4 * ntiles, 256, 24 * cn,
                                         sizeof(sphx::StepParams) * csc, 4 * (csc + 1),
                                         4 * (csc + 1), 8ull * sphx::large_list_cap((uint32_t)cn),
-                                        32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn};
+                                        32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn,
+                                        4 * (csc + 1), 4 * (cs + 1)};
     Layout L;
     size_t o = 0;
     for (int k = 0; k < Layout::kNum; ++k) {
@@ -207,6 +208,8 @@ void bind(sphx_handle *h, char *a, const Layout &L) {
     h->fr = (float4 *)(a + L.off[Layout::kFr]);
     h->nbr = (uint32_t *)(a + L.off[Layout::kNbr]);
     h->ncount = (uint32_t *)(a + L.off[Layout::kNcount]);
+    h->d_rofs = (uint32_t *)(a + L.off[Layout::kRofs]);
+    h->row_warps = sphx::RowWarps{(uint32_t *)(a + L.off[Layout::kRowOfs])};
 }
 
 // Allocates an arena for the capacities, zeroes its counts and status.
@@ -230,15 +233,22 @@ int alloc_arena(sphx_handle *h, size_t cn, size_t cs, size_t csc, char **out, La
 
 // Scene offsets -> device tables; the constants are re-uploaded on next use.
 int upload_tables(sphx_handle *h) {
-    std::vector<uint32_t> pofs(h->scenes.size() + 1), sofs(h->scenes.size() + 1);
+    std::vector<uint32_t> pofs(h->scenes.size() + 1), sofs(h->scenes.size() + 1),
+        rofs(h->scenes.size() + 1);
+    uint32_t rows = 0;
     for (size_t k = 0; k < h->scenes.size(); ++k) {
         pofs[k] = h->scenes[k].first;
         sofs[k] = h->scenes[k].slot0;
+        rofs[k] = rows;  // cell rows (gy * gz per scene) before scene k
+        rows += (uint32_t)(h->scenes[k].grid.gy * h->scenes[k].grid.gz);
     }
     pofs.back() = h->n;
     sofs.back() = h->slots;
+    rofs.back() = rows;
+    h->rows = rows;
     SPHX_CUDA(cudaMemcpyAsync(h->d_pofs, pofs.data(), 4 * pofs.size(), cudaMemcpyHostToDevice, h->stream));
     SPHX_CUDA(cudaMemcpyAsync(h->d_sofs, sofs.data(), 4 * sofs.size(), cudaMemcpyHostToDevice, h->stream));
+    SPHX_CUDA(cudaMemcpyAsync(h->d_rofs, rofs.data(), 4 * rofs.size(), cudaMemcpyHostToDevice, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));  // host vectors go out of scope
     h->sb.slots = h->slots;
     h->params_valid = false;
@@ -343,7 +353,8 @@ cudaError_t enqueue_step(sphx_handle *h, bool reorder, int &pv, int &idc, cudaEv
     if (ev) cudaEventRecord(ev[1], st);
     const sphx::NbrList L{h->nbr, h->ncount, h->opt.neighbor_slots};
     if ((e = sphx::launch_density(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L, !reorder,
-                                  st, h->tune.density_threads)) != cudaSuccess)
+                                  st, h->tune.density_threads,
+                                  SPHX_ROW_WARPS ? &h->row_warps : nullptr)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[2], st);
     if ((e = sphx::launch_force(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L,
@@ -447,7 +458,9 @@ int sphx::run_steps(sphx_handle *h, float dt, int nsteps) {
             }
             cudaEvent_t *ev = &h->events[h->events_used];
             h->launches_per_step.resize(h->events.size() / 4);
-            h->launches_per_step[h->events_used / 4] = reorder ? 10u : 9u;  // sort 7, gather, density, force
+            // sort 7, gather, row warps (1, 2 past 4095 rows), density, force
+            h->launches_per_step[h->events_used / 4] =
+                (reorder ? 10u : 9u) + (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
             h->events_used += 4;
             int pv = h->pv, idc = h->idc;
             SPHX_CUDA(enqueue_step(h, reorder, pv, idc, ev));

@@ -174,6 +174,10 @@ struct SceneTable {
     const uint32_t *sofs;
     uint32_t nscenes;
     uint32_t n;  // total particles
+    // nscenes + 1 offsets of each scene's first cell row (gy * gz rows of gx
+    // slots each); NULL where rows are not used
+    const uint32_t *rofs = nullptr;
+    uint32_t rows = 0;  // cell rows of all scenes
 };
 
 }  // namespace sphx

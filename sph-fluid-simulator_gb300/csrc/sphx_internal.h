@@ -76,6 +76,9 @@ struct sphx_handle {
     sphx::StepParams *d_params = nullptr;  // one entry per scene
     uint32_t *d_pofs = nullptr;            // scenes + 1 particle offsets
     uint32_t *d_sofs = nullptr;            // scenes + 1 slot offsets
+    uint32_t *d_rofs = nullptr;            // scenes + 1 cell-row offsets
+    uint32_t rows = 0;                     // cell rows of all scenes
+    sphx::RowWarps row_warps{};            // density warps aligned to cell rows
     std::vector<sphx::StepParams> params;  // last uploaded table
     float params_dt = 0.f;
     bool params_valid = false;
@@ -95,7 +98,8 @@ struct sphx_handle {
 namespace sphx {
 
 inline SceneTable table_of(const sphx_handle *h) {
-    return SceneTable{h->d_params, h->d_pofs, h->d_sofs, (uint32_t)h->scenes.size(), h->n};
+    return SceneTable{h->d_params, h->d_pofs,  h->d_sofs, (uint32_t)h->scenes.size(), h->n,
+                      h->d_rofs,   h->rows};
 }
 
 // A scene to place in a handle: host state (pos3/vel3, vel3 may be NULL),

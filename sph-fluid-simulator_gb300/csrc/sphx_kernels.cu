@@ -801,6 +801,101 @@ struct PosScan {
     }
 };
 
+// ---------------------------------------------------------------- row warps
+
+// The cooperative walk shares a warp's loads among lanes of the same cell
+// row; a warp whose particles straddle two rows walks them as two groups,
+// one after the other, with half its lanes idle each time.  So the density
+// pass gives every warp the particles of one row only: row R's particles
+// [start[first], start[first + gx]) go to ceil(count / 32) warps, numbered
+// from wofs[R], an exclusive scan of those counts over all rows (entry rows
+// is the total).  Lanes past a row's end idle.
+
+// Scene of global cell row R: the last s with rofs[s] <= R.
+__device__ __forceinline__ uint32_t scene_of_row(const SceneTable &T, uint32_t R) {
+    if (T.nscenes == 1) return 0;
+    uint32_t lo = 0, hi = T.nscenes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (T.rofs[mid] <= R) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// First slot of row R (of scene sc).
+__device__ __forceinline__ uint32_t row_first_slot(const SceneTable &T, uint32_t sc, uint32_t R) {
+    return T.sofs[sc] + (R - T.rofs[sc]) * (uint32_t)T.params[sc].grid.gx;
+}
+
+// Row of warp w (< wofs[rows]): the last R < rows with wofs[R] <= w, which
+// has warps, since a row after it with the same offset has none.  A 32-way
+// search, the whole warp calling with the same w: each round every lane
+// tests one point of [lo, hi) and the range shrinks to the gap after the
+// last point that passed; wofs[lo] <= w throughout.
+__device__ __forceinline__ uint32_t row_of_warp(const uint32_t *__restrict__ wofs, uint32_t rows,
+                                                uint32_t w) {
+    const uint32_t lane = threadIdx.x & 31u;
+    uint32_t lo = 0, hi = rows;
+    while (hi - lo > 1) {
+        const uint32_t stride = (hi - lo + 31u) >> 5;
+        const uint32_t x = lo + lane * stride;
+        const unsigned b = __ballot_sync(0xffffffffu, x < hi && __ldg(wofs + x) <= w);
+        lo += (uint32_t)(31 - __clz(b)) * stride;  // lane 0 always passes
+        hi = min(lo + stride, hi);
+    }
+    return lo;
+}
+
+// Kernel 1, kScanTile rows per block: every row's warp count, scanned within
+// the block into wofs, and the block's total into tile_sum.  After an error
+// no row has warps.
+__global__ void k_row_warps(SceneTable T, const uint32_t *__restrict__ start,
+                            uint32_t *__restrict__ wofs, uint32_t *__restrict__ tile_sum,
+                            const uint32_t *__restrict__ status) {
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    const bool err = status[0] & kStatusErrorMask;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const uint32_t R = base + k;
+        v[k] = 0u;
+        if (R < T.rows && !err) {
+            const uint32_t sc = scene_of_row(T, R);
+            const uint32_t f = row_first_slot(T, sc, R);
+            v[k] = (start[f + (uint32_t)T.params[sc].grid.gx] - start[f] + 31u) >> 5;
+        }
+        s += v[k];
+    }
+    uint32_t excl;
+    const uint32_t tot = block_exclusive_scan(s, excl);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k <= T.rows) wofs[base + k] = excl;
+        excl += v[k];
+    }
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+// Kernel 2 (more than one block of rows): adds the earlier blocks' totals.
+__global__ void k_row_offsets(uint32_t rows, uint32_t *__restrict__ wofs,
+                              const uint32_t *__restrict__ tile_sum) {
+    __shared__ uint32_t s_prefix;
+    if (threadIdx.x < 32) {
+        uint32_t p = 0;
+        for (uint32_t b = threadIdx.x; b < blockIdx.x; b += 32) p += tile_sum[b];
+#pragma unroll
+        for (int d = 16; d; d >>= 1) p += __shfl_xor_sync(0xffffffffu, p, d);
+        if (threadIdx.x == 0) s_prefix = p;
+    }
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k)
+        if (base + k <= rows) wofs[base + k] += s_prefix;
+}
+
 // ---------------------------------------------------------------- physics
 
 // Compensated (Kahan) accumulation: the GPU sums the same terms as the
@@ -863,13 +958,29 @@ constexpr uint32_t kNoList = 0x80000000u;
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
-              float4 *__restrict__ fr, NbrList L, const uint32_t *__restrict__ status) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+              float4 *__restrict__ fr, NbrList L, RowWarps RW,
+              const uint32_t *__restrict__ status) {
+    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     // whole warps leave together: the cooperative walk needs every lane
-    if ((t & ~31u) >= T.n || (status[0] & kStatusErrorMask)) return;
-    const bool valid = t < T.n;
+    if (status[0] & kStatusErrorMask) return;
+    uint32_t t;  // cell-sorted position of this thread's particle
+    bool valid;
+    uint32_t sc = 0;
+    if (RW.wofs) {  // one cell row per warp
+        const uint32_t w = g >> 5;
+        if (w >= RW.wofs[T.rows]) return;
+        const uint32_t R = row_of_warp(RW.wofs, T.rows, w);
+        sc = scene_of_row(T, R);
+        const uint32_t f = row_first_slot(T, sc, R);
+        t = G.start[f] + ((w - RW.wofs[R]) << 5) + (threadIdx.x & 31u);
+        valid = t < G.start[f + (uint32_t)T.params[sc].grid.gx];
+    } else {
+        if ((g & ~31u) >= T.n) return;
+        t = g;
+        valid = t < T.n;
+    }
     const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
-    const uint32_t sc = valid ? scene_of(T, i) : 0u;
+    if (!RW.wofs) sc = valid ? scene_of(T, i) : 0u;
     const StepParams &P = T.params[sc];
     const WalkCtx W = walk_ctx(T, G, sc, P, status);
     const float4 pi = W.pos[i];
@@ -1431,21 +1542,31 @@ static WalkCtx global_ctx(const SortBuffers &B, const float4 *pos) {
 
 template <int kThreads>
 static void density_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel, float4 *rp,
-                           float4 *fr, const NbrList &L, bool indirect, const uint32_t *status,
-                           cudaStream_t st) {
+                           float4 *fr, const NbrList &L, const RowWarps &RW, bool indirect,
+                           const uint32_t *status, cudaStream_t st) {
+    // with row warps: at most n / 32 + rows warps (each row's last is partial)
+    const uint32_t threads = RW.wofs ? (T.n / 32u + T.rows + 1u) * 32u : T.n;
     if (indirect)
-        k_density<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, status);
+        k_density<true, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, RW, status);
     else
-        k_density<false, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, status);
+        k_density<false, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, RW, status);
 }
 
 cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                            const float4 *vel, float4 *rp, float4 *fr, const NbrList &L,
-                           bool indirect, cudaStream_t st, int threads) {
+                           bool indirect, cudaStream_t st, int threads, const RowWarps *rw) {
     const WalkCtx G = global_ctx(B, pos);
+    RowWarps RW{nullptr};
+    if (T.n && rw && T.rofs && T.rows) {
+        // rows + 1 scan entries; the sort's tile sums are free again
+        const uint32_t ntiles = (T.rows + 1 + kScanTile - 1) / kScanTile;
+        k_row_warps<<<ntiles, kScanThreads, 0, st>>>(T, B.start, rw->wofs, B.tile_sum, B.status);
+        if (ntiles > 1) k_row_offsets<<<ntiles, kScanThreads, 0, st>>>(T.rows, rw->wofs, B.tile_sum);
+        RW = *rw;
+    }
     if (T.n) {
-        if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, indirect, B.status, st);
-        else density_launch<256>(T, G, vel, rp, fr, L, indirect, B.status, st);
+        if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, RW, indirect, B.status, st);
+        else density_launch<256>(T, G, vel, rp, fr, L, RW, indirect, B.status, st);
     }
     return cudaGetLastError();
 }

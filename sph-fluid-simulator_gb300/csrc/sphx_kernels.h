@@ -59,11 +59,23 @@ struct NbrList {
 };
 constexpr uint32_t kNbrSlotsDefault = 256, kNbrSlotsMax = 1024;
 
+// The density pass's warps, each inside one cell row (see k_row_warps):
+// wofs[R] = first warp of cell row R, rows + 1 entries.
+#ifndef SPHX_ROW_WARPS
+#define SPHX_ROW_WARPS 1
+#endif
+struct RowWarps {
+    uint32_t *wofs;
+};
+
 // fr: 2 float4 per particle, (x, y, z, p) and (vx, vy, vz, 1/rho), written
-// by the density kernel when L.nbr is set (vel then required).
+// by the density kernel when fr is set (vel then required).  With rw (and
+// T.rofs), each warp of the pass takes particles of one cell row only; else
+// consecutive threads take consecutive cell-sorted particles.
 cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                            const float4 *vel, float4 *rp, float4 *fr, const NbrList &L,
-                           bool indirect, cudaStream_t st, int threads = 256);
+                           bool indirect, cudaStream_t st, int threads = 256,
+                           const RowWarps *rw = nullptr);
 cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                          const float4 *vel, const float4 *rp, const float4 *fr, const NbrList &L,
                          float4 *pos_out, float4 *vel_out, float4 *force_out, bool indirect,
