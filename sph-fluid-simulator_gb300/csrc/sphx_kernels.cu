@@ -847,6 +847,36 @@ __device__ __forceinline__ uint32_t row_of_warp(const uint32_t *__restrict__ wof
     return lo;
 }
 
+// Thread g's particle: its cell-sorted position t, whether it has one
+// (valid) and, with row warps, its scene.  False when the whole warp has
+// nothing to do (the cooperative walk needs every lane, so warps leave
+// together).
+__device__ __forceinline__ bool thread_particle(const SceneTable &T, const uint32_t *__restrict__ start,
+                                                const RowWarps &RW, uint32_t g, uint32_t &t,
+                                                bool &valid, uint32_t &sc) {
+    sc = 0;
+    if (RW.wofs) {  // one cell row per warp
+        const uint32_t w = g >> 5;
+        if (w >= RW.wofs[T.rows]) return false;
+        const uint32_t R = row_of_warp(RW.wofs, T.rows, w);
+        sc = scene_of_row(T, R);
+        const uint32_t f = row_first_slot(T, sc, R);
+        t = start[f] + ((w - RW.wofs[R]) << 5) + (threadIdx.x & 31u);
+        valid = t < start[f + (uint32_t)T.params[sc].grid.gx];
+        return true;
+    }
+    if ((g & ~31u) >= T.n) return false;
+    t = g;
+    valid = t < T.n;
+    return true;
+}
+
+// Threads a launch needs: with row warps at most n / 32 + rows warps (a
+// row's last warp is partial).
+__host__ __forceinline__ uint32_t launch_threads(const SceneTable &T, const RowWarps &RW) {
+    return RW.wofs ? (T.n / 32u + T.rows + 1u) * 32u : T.n;
+}
+
 // Kernel 1, kScanTile rows per block: every row's warp count, scanned within
 // the block into wofs, and the block's total into tile_sum.  After an error
 // no row has warps.
@@ -960,25 +990,10 @@ __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThrea
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
               float4 *__restrict__ fr, NbrList L, RowWarps RW,
               const uint32_t *__restrict__ status) {
-    const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-    // whole warps leave together: the cooperative walk needs every lane
     if (status[0] & kStatusErrorMask) return;
-    uint32_t t;  // cell-sorted position of this thread's particle
+    uint32_t t, sc;
     bool valid;
-    uint32_t sc = 0;
-    if (RW.wofs) {  // one cell row per warp
-        const uint32_t w = g >> 5;
-        if (w >= RW.wofs[T.rows]) return;
-        const uint32_t R = row_of_warp(RW.wofs, T.rows, w);
-        sc = scene_of_row(T, R);
-        const uint32_t f = row_first_slot(T, sc, R);
-        t = G.start[f] + ((w - RW.wofs[R]) << 5) + (threadIdx.x & 31u);
-        valid = t < G.start[f + (uint32_t)T.params[sc].grid.gx];
-    } else {
-        if ((g & ~31u) >= T.n) return;
-        t = g;
-        valid = t < T.n;
-    }
+    if (!thread_particle(T, G.start, RW, blockIdx.x * blockDim.x + threadIdx.x, t, valid, sc)) return;
     const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
     if (!RW.wofs) sc = valid ? scene_of(T, i) : 0u;
     const StepParams &P = T.params[sc];
@@ -1545,7 +1560,7 @@ static void density_launch(const SceneTable &T, const WalkCtx &G, const float4 *
                            float4 *fr, const NbrList &L, const RowWarps &RW, bool indirect,
                            const uint32_t *status, cudaStream_t st) {
     // with row warps: at most n / 32 + rows warps (each row's last is partial)
-    const uint32_t threads = RW.wofs ? (T.n / 32u + T.rows + 1u) * 32u : T.n;
+    const uint32_t threads = launch_threads(T, RW);
     if (indirect)
         k_density<true, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, RW, status);
     else
