@@ -953,7 +953,9 @@ struct DensityVisitor {
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float d2) {
         const float u = __fsub_rn(h2, d2);
         kahan_add(acc, comp, __fmul_rn(__fmul_rn(u, u), u));
-        if (row && cnt < slots) row[cnt] = j;
+        // streaming store: the force pass reads the row once, after every
+        // other row has been written
+        if (row && cnt < slots) __stcs(row + cnt, j);
         ++cnt;
     }
 };
