@@ -157,7 +157,7 @@ struct Layout {
     enum {
         kPos0, kPos1, kVel0, kVel1, kId0, kId1, kRp, kForce, kKey, kRank, kOrder, kCount,
         kStart, kTiles, kStatus, kStaging, kParams, kPofs, kSofs, kLarge, kFr, kNbr, kNcount,
-        kScat, kRofs, kRowOfs, kNum
+        kScat, kRofs, kRowOfs, kDeferred, kNum
     };
     size_t off[kNum];
     size_t total;
@@ -171,7 +171,7 @@ Layout layout_for(size_t cn, size_t cs, size_t csc, size_t slots) {
                                         sizeof(sphx::StepParams) * csc, 4 * (csc + 1),
                                         4 * (csc + 1), 8ull * sphx::large_list_cap((uint32_t)cn),
                                         32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn,
-                                        4 * (csc + 1), 4 * (cs + 1)};
+                                        4 * (csc + 1), 4 * (cs + 1), 8 * cn};
     Layout L;
     size_t o = 0;
     for (int k = 0; k < Layout::kNum; ++k) {
@@ -205,6 +205,7 @@ void bind(sphx_handle *h, char *a, const Layout &L) {
     h->d_pofs = (uint32_t *)(a + L.off[Layout::kPofs]);
     h->d_sofs = (uint32_t *)(a + L.off[Layout::kSofs]);
     h->sb.large = (uint2 *)(a + L.off[Layout::kLarge]);
+    h->sb.deferred = (uint32_t *)(a + L.off[Layout::kDeferred]);
     h->fr = (float4 *)(a + L.off[Layout::kFr]);
     h->nbr = (uint32_t *)(a + L.off[Layout::kNbr]);
     h->ncount = (uint32_t *)(a + L.off[Layout::kNcount]);
@@ -458,9 +459,10 @@ int sphx::run_steps(sphx_handle *h, float dt, int nsteps) {
             }
             cudaEvent_t *ev = &h->events[h->events_used];
             h->launches_per_step.resize(h->events.size() / 4);
-            // sort 7, gather, row warps (1, 2 past 4095 rows), density, force
+            // sort 7, gather, row warps (1, 2 past 4095 rows), density and
+            // force with their deferred-particle companions
             h->launches_per_step[h->events_used / 4] =
-                (reorder ? 10u : 9u) + (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
+                (reorder ? 12u : 11u) + (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
             h->events_used += 4;
             int pv = h->pv, idc = h->idc;
             SPHX_CUDA(enqueue_step(h, reorder, pv, idc, ev));

@@ -57,15 +57,45 @@ SPHX_HD int trunc_to_int(float q) {
 #endif
 }
 
+#if defined(__CUDA_ARCH__)
+#define SPHX_UNROLL _Pragma("unroll")
+#else
+#define SPHX_UNROLL
+#endif
+
 // xor-basis insertion ("x = min(x, x ^ b)" over the basis in insertion order
-// keeps every element reduced at the leading bits of the earlier ones).
-SPHX_HD uint32_t reduce6(uint32_t x, const uint32_t *b, int nb) {
-    for (int k = 0; k < 6; ++k)
-        if (k < nb) {
-            const uint32_t y = x ^ b[k];
-            x = y < x ? y : x;
-        }
+// keeps every element reduced at the leading bits of the earlier ones).  The
+// basis has a fixed slot per inserted vector, 0 for one that reduced to 0:
+// x ^ 0 = x, so such a slot changes no later reduction, and with constant
+// indexes the basis stays in registers.
+template <int kN>
+SPHX_HD uint32_t reduce_basis(uint32_t x, const uint32_t *b) {
+    SPHX_UNROLL
+    for (int k = 0; k < kN; ++k) {
+        const uint32_t y = x ^ b[k];
+        x = y < x ? y : x;
+    }
     return x;
+}
+
+// Whether one of the nine cells two steps across face `face` (-x, +x, -y,
+// +y, -z, +z) has the bucket of one of the 27 cells around the centre; A, B,
+// C hold the low 16 bits of the axis products at offsets -2..2.  In the
+// face's frame (u across it, v and w along it, as the slow walk steps them)
+// a bucket is the xor of three axis terms.
+SPHX_HD bool face_collides(const uint32_t *A, const uint32_t *B, const uint32_t *C, int face) {
+    const int axis = face >> 1, far = (face & 1) ? 4 : 0;
+    const uint32_t *P[3] = {A, B, C};
+    const uint32_t *U = P[axis], *V = P[(axis + 1) % 3], *W = P[(axis + 2) % 3];
+    for (int v = 1; v <= 3; ++v)
+        for (int w = 1; w <= 3; ++w) {
+            const uint32_t hf = U[far] ^ V[v] ^ W[w];
+            for (int u = 1; u <= 3; ++u)
+                for (int v2 = 1; v2 <= 3; ++v2)
+                    for (int w2 = 1; w2 <= 3; ++w2)
+                        if ((U[u] ^ V[v2] ^ W[w2]) == hf) return true;
+        }
+    return false;
 }
 
 // Bucket-collision structure of the 27 cells around (cx, cy, cz).
@@ -79,8 +109,8 @@ SPHX_HD uint32_t reduce6(uint32_t x, const uint32_t *b, int nb) {
 // A cell two steps away across the +x face, (cx+2, cy+dy, cz+dz), can share
 // a bucket with one of the 27 only if A[1]^A[2] lies in the span of the six
 // vectors (necessary, not sufficient); likewise for the other five faces.
-// The matching face bit is set conservatively; the walk then checks the
-// actual hashes of the nine cells of that face.
+// Only then are the nine cells of that face compared with the 27 buckets,
+// and the face bit is set iff one of them matches: exact, like kFlagDup.
 SPHX_HD uint32_t collision_flags(int cx, int cy, int cz, uint32_t face_mask) {
     uint32_t A[5], B[5], C[5];
     for (int k = 0; k < 5; ++k) {
@@ -91,18 +121,21 @@ SPHX_HD uint32_t collision_flags(int cx, int cy, int cz, uint32_t face_mask) {
     const uint32_t v[6] = {A[1] ^ A[2], A[2] ^ A[3], B[1] ^ B[2],
                            B[2] ^ B[3], C[1] ^ C[2], C[2] ^ C[3]};
     uint32_t basis[6];
-    int nb = 0;
-    uint32_t flags = 0;
-    for (int i = 0; i < 6; ++i) {
-        const uint32_t x = reduce6(v[i], basis, nb);
-        if (x == 0u) flags |= kFlagDup;
-        else basis[nb++] = x;
-    }
+    basis[0] = v[0];
+    basis[1] = reduce_basis<1>(v[1], basis);
+    basis[2] = reduce_basis<2>(v[2], basis);
+    basis[3] = reduce_basis<3>(v[3], basis);
+    basis[4] = reduce_basis<4>(v[4], basis);
+    basis[5] = reduce_basis<5>(v[5], basis);
+    uint32_t flags = (basis[0] && basis[1] && basis[2] && basis[3] && basis[4] && basis[5]) ? 0u : kFlagDup;
     const uint32_t f[6] = {A[0] ^ A[1], A[3] ^ A[4], B[0] ^ B[1],
                            B[3] ^ B[4], C[0] ^ C[1], C[3] ^ C[4]};
+    // the span test first: it rules out almost every face at once
+    SPHX_UNROLL
     for (int i = 0; i < 6; ++i)
         if ((face_mask >> i) & 1u)
-            if (reduce6(f[i], basis, nb) == 0u) flags |= 1u << (kFlagFaceShift + i);
+            if (reduce_basis<6>(f[i], basis) == 0u && face_collides(A, B, C, i))
+                flags |= 1u << (kFlagFaceShift + i);
     return flags;
 }
 

@@ -494,39 +494,33 @@ __device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, in
     }
 }
 
-template <bool kInd, class V>
-__device__ __forceinline__ void walk_cell(const WalkCtx &W, int cx, int cy, int cz, uint32_t self,
-                                          float4 pi, uint32_t w, V &vis) {
-    int mx, my, mz;
-    const uint32_t k = slot_of(W.grid, cx, cy, cz, mx, my, mz);
-    scan_run<kInd>(W, W.start[k], W.start[k + 1], self, pi, w, vis);
-}
-
 // Slow path, taken when `flags` reports a bucket collision: every neighbour
 // cell is walked with weight = number of the 27 offsets whose bucket equals
 // its bucket (the reference walks a bucket once per offset that hashes to it,
 // sph.cpp:40-63), and, for each flagged face, the nine cells two steps away
 // whose bucket is among the 27 are walked with that same weight.
-template <bool kInd, class V>
-__device__ __noinline__ void walk_slow(const WalkCtx &W, int cx, int cy, int cz, uint32_t flags,
-                                       uint32_t self, float4 pi, V &vis) {
+// slow_cells calls f(slot, weight) for those cells, in walk order.
+template <class F>
+__device__ __forceinline__ void slow_cells(const Grid &g, int cx, int cy, int cz, uint32_t flags,
+                                           F &&f) {
     uint32_t H[27];
     int o = 0;
     for (int x = -1; x <= 1; ++x)
         for (int y = -1; y <= 1; ++y)
             for (int z = -1; z <= 1; ++z) H[o++] = hash16(cx + x, cy + y, cz + z);
+    int mx, my, mz;
     o = 0;
     for (int x = -1; x <= 1; ++x)
         for (int y = -1; y <= 1; ++y)
             for (int z = -1; z <= 1; ++z) {
                 uint32_t w = 0;
                 for (int k = 0; k < 27; ++k) w += H[k] == H[o] ? 1u : 0u;
-                walk_cell<kInd>(W, cx + x, cy + y, cz + z, self, pi, w, vis);
+                f(slot_of(g, cx + x, cy + y, cz + z, mx, my, mz), w);
                 ++o;
             }
-    for (int f = 0; f < 6; ++f) {
-        if (!((flags >> (kFlagFaceShift + f)) & 1u)) continue;
-        const int axis = f >> 1, step = (f & 1) ? 2 : -2;
+    for (int fc = 0; fc < 6; ++fc) {
+        if (!((flags >> (kFlagFaceShift + fc)) & 1u)) continue;
+        const int axis = fc >> 1, step = (fc & 1) ? 2 : -2;
         for (int a = -1; a <= 1; ++a)
             for (int b = -1; b <= 1; ++b) {
                 int c[3] = {cx, cy, cz};
@@ -536,9 +530,17 @@ __device__ __noinline__ void walk_slow(const WalkCtx &W, int cx, int cy, int cz,
                 const uint32_t hf = hash16(c[0], c[1], c[2]);
                 uint32_t w = 0;
                 for (int k = 0; k < 27; ++k) w += H[k] == hf ? 1u : 0u;
-                if (w) walk_cell<kInd>(W, c[0], c[1], c[2], self, pi, w, vis);
+                if (w) f(slot_of(g, c[0], c[1], c[2], mx, my, mz), w);
             }
     }
+}
+
+template <bool kInd, class V>
+__device__ __noinline__ void walk_slow(const WalkCtx &W, int cx, int cy, int cz, uint32_t flags,
+                                       uint32_t self, float4 pi, V &vis) {
+    slow_cells(W.grid, cx, cy, cz, flags, [&](uint32_t k, uint32_t w) {
+        scan_run<kInd>(W, W.start[k], W.start[k + 1], self, pi, w, vis);
+    });
 }
 
 // Cell, slot and collision flags of a particle; returns true when the fast
@@ -712,11 +714,18 @@ __device__ __forceinline__ void coop_rows_warp(const WalkCtx &W, const WalkStart
     }
 }
 
+// What coop_walk does with the valid lanes off the cooperative path: walk
+// them alone with `vis` (kTailAll), walk them alone when they need no bucket
+// weights, i.e. sit at the grid's x seam (kTailRows: the caller has handed
+// the others to a later kernel), or leave them all to the caller
+// (kTailNone).  Keeping the slow walk, a call, out of a kernel frees its
+// register allocation.
+enum CoopTail { kTailNone, kTailRows, kTailAll };
+
 // Runs the scanner over every fast lane's neighbours, one group after
-// another (kWarpLoad: coop_rows_warp, else coop_rows_group); the lanes off
-// the fast path then walk alone with `vis`.  Every lane of the warp calls it
-// (lanes without a walk pass valid = false).
-template <bool kInd, bool kWarpLoad, class S, class V>
+// another (kWarpLoad: coop_rows_warp, else coop_rows_group), then the tail.
+// Every lane of the warp calls it (lanes without a walk pass valid = false).
+template <bool kInd, bool kWarpLoad, int kTail, class S, class V>
 __device__ __forceinline__ void coop_walk(const WalkCtx &W, const WalkStart &s, const CoopLane &cl,
                                           uint32_t self, float4 pi, S &scan, V &vis) {
     const uint32_t lane = threadIdx.x & 31u;
@@ -735,7 +744,22 @@ __device__ __forceinline__ void coop_walk(const WalkCtx &W, const WalkStart &s, 
             pending &= ~__shfl_sync(0xffffffffu, gm, leader);
         }
     }
-    if (cl.valid && !cl.fast) walk<kInd>(W, s, self, pi, vis);
+    if (kTail == kTailAll && cl.valid && !cl.fast) walk<kInd>(W, s, self, pi, vis);
+    if (kTail == kTailRows && cl.valid && !cl.fast && s.flags == 0u)
+        walk_rows<kInd>(W, s.c, s.mx, s.my, s.mz, self, pi, vis);
+}
+
+// Appends the warp's lanes with `defer` set to a deferred list (*counter
+// counts it), one atomic per warp.  Every lane of the warp calls it.
+__device__ __forceinline__ void defer_lanes(bool defer, uint32_t t, uint32_t *__restrict__ deferred,
+                                            uint32_t *__restrict__ counter) {
+    const uint32_t m = __ballot_sync(0xffffffffu, defer);
+    if (!m) return;
+    const uint32_t lane = threadIdx.x & 31u, leader = __ffs(m) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (defer) deferred[base + __popc(m & ((1u << lane) - 1u))] = t;
 }
 
 // Chunk of candidate positions; the lane's visitor sees each candidate of its
@@ -763,6 +787,12 @@ struct PosScan {
     __device__ __forceinline__ void test(const WalkCtx &W, uint32_t c0, uint32_t k, uint32_t self,
                                          float4 pi) {
         test_pair(W, kInd ? sm.idx[k] : c0 + k, sm.p(k), self, pi, 1u, vis);
+    }
+    // Every candidate of chunk slots [lo, hi), with weight w (scan_run's test).
+    __device__ __forceinline__ void test_all(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
+                                             uint32_t self, float4 pi, uint32_t w) {
+        for (uint32_t k = lo; k < hi; ++k)
+            test_pair(W, kInd ? sm.idx[k] : c0 + k, sm.p(k), self, pi, w, vis);
     }
     // Chunk slots [lo, hi), the chunk starting at cell-sorted slot c0; true
     // once past the window's end.
@@ -800,6 +830,43 @@ struct PosScan {
         return false;
     }
 };
+
+// One particle's walk by a whole warp, for the particles the walk kernels
+// defer.  The lanes copy each cell's run into the scanner's chunk, 32
+// candidates at a time, and lane 0 tests them in order: the same cells, order
+// and weights as walk() (the slow path's cells where buckets collide, else
+// the 27 cells row by row, which is walk_rows' order), so the sums are
+// walk()'s bit for bit, while the loads of a candidate run go out together
+// instead of one dependent load after another.
+template <bool kInd, class S>
+__device__ __forceinline__ void warp_walk_cell(const WalkCtx &W, uint32_t k, uint32_t w,
+                                               uint32_t self, float4 pi, S &scan) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t a = W.start[k], b = W.start[k + 1];
+#pragma unroll 1
+    for (uint32_t c0 = a; c0 < b; c0 += 32u) {
+        const uint32_t m = min(32u, b - c0);
+        if (lane < m) scan.load(W, lane, kInd ? W.order[c0 + lane] : c0 + lane);
+        __syncwarp();
+        if (lane == 0) scan.test_all(W, c0, 0u, m, self, pi, w);
+        __syncwarp();
+    }
+}
+
+template <bool kInd, class S>
+__device__ __forceinline__ void warp_walk(const WalkCtx &W, const WalkStart &s, uint32_t self,
+                                          float4 pi, S &scan) {
+    auto cell = [&](uint32_t k, uint32_t w) { warp_walk_cell<kInd>(W, k, w, self, pi, scan); };
+    if (s.flags != 0u) {
+        slow_cells(W.grid, s.c.cx, s.c.cy, s.c.cz, s.flags, cell);
+        return;
+    }
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        const uint32_t base = row_base(W.grid, s.my, s.mz, r);
+        for (int dx = -1; dx <= 1; ++dx) cell(base + (uint32_t)wrap1(s.mx + dx, W.grid.gx), 1u);
+    }
+}
 
 // ---------------------------------------------------------------- row warps
 
@@ -973,9 +1040,10 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
     return W;
 }
 
-#ifndef SPHX_DENSITY_COOP
-#define SPHX_DENSITY_COOP 1
-#endif
+// Threads and blocks of the kernels that take the deferred particles: few
+// in fluid (none in the dam-break block), at most n.
+constexpr int kDeferredThreads = 128;
+constexpr unsigned kDeferredBlocks = 2 * 152;
 // No list is recorded for a particle whose cell holds more than
 // slots / kListSkipFactor particles; its count then carries kNoList.
 #ifndef SPHX_LIST_SKIP_FACTOR
@@ -984,14 +1052,47 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
 constexpr uint32_t kListSkipFactor = SPHX_LIST_SKIP_FACTOR;
 constexpr uint32_t kNoList = 0x80000000u;
 
+// A particle's list row, or NULL when its own cell holds so many particles
+// (clumped fluid) that it has more neighbours than the row holds and the
+// force pass walks for it: recording them would only cost writes.  Either
+// way the force is the same.
+__device__ __forceinline__ uint32_t *density_row(const WalkCtx &W, const WalkStart &s,
+                                                 const NbrList &L, uint32_t i) {
+    if (!L.nbr) return nullptr;
+    const uint32_t k = ((uint32_t)s.mz * (uint32_t)W.grid.gy + (uint32_t)s.my) *
+                           (uint32_t)W.grid.gx + (uint32_t)s.mx;
+    const uint32_t occ = W.start[k + 1] - W.start[k];
+    return occ * kListSkipFactor <= L.slots ? L.nbr + (size_t)i * L.slots : nullptr;
+}
+
+// Density, pressure, the list count and the neighbour record of particle i.
+__device__ __forceinline__ void density_finish(const StepParams &P, const DensityVisitor &v,
+                                               uint32_t i, float4 pi, const float4 *__restrict__ vel,
+                                               float4 *__restrict__ rp, float4 *__restrict__ fr,
+                                               const NbrList &L) {
+    const float rho = __fadd_rn(__fmul_rn(P.mp6, v.acc), P.selfDens);
+    const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
+    const float inv = __frcp_rn(rho);
+    rp[i] = make_float4(rho, prs, inv, 0.f);
+    if (L.nbr) L.count[i] = v.row ? v.cnt : (v.cnt | kNoList);
+    if (fr) {
+        // what the force kernel reads of a neighbour, in one 32-byte record
+        const float4 vi = vel[i];
+        fr[2 * (size_t)i] = make_float4(pi.x, pi.y, pi.z, prs);
+        fr[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, inv);
+    }
+}
+
 // Density and pressure, sph.cpp:28-76.  The reference accumulates
 // m*poly6*(h^2-r^2)^3 term by term; here the cubes are summed (compensated)
-// and scaled once: the two differ by float rounding only.
+// and scaled once: the two differ by float rounding only.  Particles whose
+// neighbourhood has a bucket collision are listed in `deferred` for
+// k_density_deferred.
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
-              float4 *__restrict__ fr, NbrList L, RowWarps RW,
-              const uint32_t *__restrict__ status) {
+              float4 *__restrict__ fr, NbrList L, RowWarps RW, uint32_t *__restrict__ deferred,
+              uint32_t *__restrict__ status) {
     if (status[0] & kStatusErrorMask) return;
     uint32_t t, sc;
     bool valid;
@@ -1003,35 +1104,39 @@ __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThrea
     const float4 pi = W.pos[i];
     WalkStart s;
     walk_start(P, pi, s);
-    uint32_t *row = nullptr;
-    if (valid && L.nbr) {
-        // A particle of a crowded cell (clumped fluid) has more neighbours
-        // than its list holds, and the force pass walks for it: recording
-        // them would only cost writes.  Either way the force is the same.
-        const uint32_t k = ((uint32_t)s.mz * (uint32_t)W.grid.gy + (uint32_t)s.my) *
-                               (uint32_t)W.grid.gx + (uint32_t)s.mx;
-        const uint32_t occ = W.start[k + 1] - W.start[k];
-        if (occ * kListSkipFactor <= L.slots) row = L.nbr + (size_t)i * L.slots;
-    }
-    DensityVisitor v{P.h2, 0.f, 0.f, row, L.slots, 0u};
-#if SPHX_DENSITY_COOP
+    const bool slow = valid && s.flags != 0u;
+    defer_lanes(slow, t, deferred, &status[kStatusDeferred]);
+    DensityVisitor v{P.h2, 0.f, 0.f, valid && !slow ? density_row(W, s, L, i) : nullptr, L.slots, 0u};
     __shared__ PosSmem<kInd> s_coop[kThreads / 32];
     PosScan<kInd, DensityVisitor> scan{s_coop[threadIdx.x >> 5], v};
-    coop_walk<kInd, false>(W, s, coop_lane(valid, sc, W, s), i, pi, scan, v);
-#else
-    if (valid) walk<kInd>(W, s, i, pi, v);
-#endif
-    if (!valid) return;
-    const float rho = __fadd_rn(__fmul_rn(P.mp6, v.acc), P.selfDens);
-    const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
-    const float inv = __frcp_rn(rho);
-    rp[i] = make_float4(rho, prs, inv, 0.f);
-    if (L.nbr) L.count[i] = row ? v.cnt : (v.cnt | kNoList);
-    if (fr) {
-        // what the force kernel reads of a neighbour, in one 32-byte record
-        const float4 vi = vel[i];
-        fr[2 * (size_t)i] = make_float4(pi.x, pi.y, pi.z, prs);
-        fr[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, inv);
+    coop_walk<kInd, false, kTailRows>(W, s, coop_lane(valid, sc, W, s), i, pi, scan, v);
+    if (valid && !slow) density_finish(P, v, i, pi, vel, rp, fr, L);
+}
+
+// The particles k_density deferred, one warp each (warp_walk).
+template <bool kInd>
+__global__ void __launch_bounds__(kDeferredThreads)
+    k_density_deferred(SceneTable T, WalkCtx G, const float4 *__restrict__ vel,
+                       float4 *__restrict__ rp, float4 *__restrict__ fr, NbrList L,
+                       const uint32_t *__restrict__ deferred, const uint32_t *__restrict__ status) {
+    if (status[0] & kStatusErrorMask) return;
+    __shared__ PosSmem<kInd> s_chunk[kDeferredThreads / 32];
+    const uint32_t m = status[kStatusDeferred];
+    const uint32_t lane = threadIdx.x & 31u, nw = gridDim.x * (kDeferredThreads / 32);
+#pragma unroll 1
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < m; q += nw) {
+        const uint32_t t = deferred[q];
+        const uint32_t i = kInd ? G.order[t] : t;
+        const uint32_t sc = scene_of(T, i);
+        const StepParams &P = T.params[sc];
+        const WalkCtx W = walk_ctx(T, G, sc, P, status);
+        const float4 pi = W.pos[i];
+        WalkStart s;
+        walk_start(P, pi, s);
+        DensityVisitor v{P.h2, 0.f, 0.f, lane == 0 ? density_row(W, s, L, i) : nullptr, L.slots, 0u};
+        PosScan<kInd, DensityVisitor> scan{s_chunk[threadIdx.x >> 5], v};
+        warp_walk<kInd>(W, s, i, pi, scan);
+        if (lane == 0) density_finish(P, v, i, pi, vel, rp, fr, L);
     }
 }
 
@@ -1128,6 +1233,21 @@ struct RecordScan {
         sm.b[k] = fr[2 * (size_t)j + 1];
         if (kInd) sm.idx[k] = j;
     }
+    // Every candidate of chunk slots [lo, hi), with weight w: the pairs of
+    // ForceVisitor under scan_run, from the chunk's records.
+    __device__ __forceinline__ void test_all(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
+                                             uint32_t self, float4 pi, uint32_t w) {
+        for (uint32_t k = lo; k < hi; ++k) {
+            const float4 p = sm.a[k];
+            const float dx = __fsub_rn(p.x, pi.x);
+            const float dy = __fsub_rn(p.y, pi.y);
+            const float dz = __fsub_rn(p.z, pi.z);
+            const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            const uint32_t j = kInd ? sm.idx[k] : c0 + k;
+            if (d2 < W.h2 && j != self)
+                for (uint32_t r = 0; r < w; ++r) pair_add_record(pair, p, sm.b[k], pi);
+        }
+    }
     __device__ __forceinline__ bool scan(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
                                          float xlo, float xhi, uint32_t self, float4 pi) {
         bool done = false;
@@ -1211,6 +1331,20 @@ __device__ __forceinline__ void integrate(const StepParams &P, float4 &x, float4
     }
 }
 
+// Force, then integration and walls, of particle i (density rho).
+__device__ __forceinline__ void force_finish(const StepParams &P, const ForcePair &pair, uint32_t i,
+                                             float4 pi, float4 vi, float rho,
+                                             float4 *__restrict__ pos_out,
+                                             float4 *__restrict__ vel_out,
+                                             float4 *__restrict__ force_out) {
+    const float fx = pair.fx, fy = pair.fy, fz = pair.fz;
+    force_out[i] = make_float4(fx, fy, fz, 0.f);
+    float4 x = pi, v = vi;
+    integrate(P, x, v, fx, fy, fz, rho);
+    pos_out[i] = x;
+    vel_out[i] = v;
+}
+
 // Force of every particle: over its list when its neighbours fit one (same
 // neighbours, same order as the density walk), else by a warp-cooperative
 // walk over the neighbour records in that same order.  Only the lanes past
@@ -1220,7 +1354,9 @@ __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
-            const uint32_t *__restrict__ status) {
+            uint32_t *__restrict__ deferred, uint32_t *__restrict__ status) {
+    // particles past their list and off the cooperative path are listed in
+    // `deferred` for k_force_deferred
     __shared__ RecordSmem<kInd> s_coop[kThreads / 32];
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     // whole warps leave together: the cooperative walk needs every lane
@@ -1261,21 +1397,51 @@ __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads
         }
     }
     const bool walker = valid && cnt > L.slots;
+    bool mine = valid;
     if (__any_sync(0xffffffffu, walker)) {
         const WalkCtx W = walk_ctx(T, G, sc, P, status);
         WalkStart s;
         walk_start(P, pi, s);
         RecordScan<kInd> scan{s_coop[threadIdx.x >> 5], fr, pair};
         ForceVisitor v{pair, fr, pi};
-        coop_walk<kInd, true>(W, s, coop_lane(walker, sc, W, s), i, pi, scan, v);
+        const CoopLane cl = coop_lane(walker, sc, W, s);
+        defer_lanes(walker && !cl.fast, t, deferred, &status[kStatusDeferredForce]);
+        coop_walk<kInd, true, kTailNone>(W, s, cl, i, pi, scan, v);
+        mine = valid && (!walker || cl.fast);
     }
-    if (!valid) return;
-    const float fx = pair.fx, fy = pair.fy, fz = pair.fz;
-    force_out[i] = make_float4(fx, fy, fz, 0.f);
-    float4 x = pi, v = vi;
-    integrate(P, x, v, fx, fy, fz, q.x);
-    pos_out[i] = x;
-    vel_out[i] = v;
+    if (mine) force_finish(P, pair, i, pi, vi, q.x, pos_out, vel_out, force_out);
+}
+
+// The particles k_force deferred, one warp each (warp_walk over the
+// neighbour records).
+template <bool kInd>
+__global__ void __launch_bounds__(kDeferredThreads)
+    k_force_deferred(SceneTable T, WalkCtx G, const float4 *__restrict__ vel,
+                     const float4 *__restrict__ rp, const float4 *__restrict__ fr, NbrList L,
+                     float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
+                     float4 *__restrict__ force_out, const uint32_t *__restrict__ deferred,
+                     const uint32_t *__restrict__ status) {
+    if (status[0] & kStatusErrorMask) return;
+    __shared__ RecordSmem<kInd> s_chunk[kDeferredThreads / 32];
+    const uint32_t m = status[kStatusDeferredForce];
+    const uint32_t lane = threadIdx.x & 31u, nw = gridDim.x * (kDeferredThreads / 32);
+#pragma unroll 1
+    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < m; q += nw) {
+        const uint32_t t = deferred[q];
+        const uint32_t i = kInd ? G.order[t] : t;
+        const uint32_t sc = scene_of(T, i);
+        const StepParams &P = T.params[sc];
+        const WalkCtx W = walk_ctx(T, G, sc, P, status);
+        const float4 pi = W.pos[i];
+        const float4 vi = vel[i];
+        const float4 r = rp[i];
+        ForcePair pair{vi, r.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        WalkStart s;
+        walk_start(P, pi, s);
+        RecordScan<kInd> scan{s_chunk[threadIdx.x >> 5], fr, pair};
+        warp_walk<kInd>(W, s, i, pi, scan);
+        if (lane == 0) force_finish(P, pair, i, pi, vi, r.x, pos_out, vel_out, force_out);
+    }
 }
 
 // ---------------------------------------------------------------- readouts
@@ -1319,7 +1485,7 @@ __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ i
     // the same walk as k_density's
     __shared__ PosSmem<kInd> s_coop[kDigestThreads / 32];
     PosScan<kInd, DigestVisitor> scan{s_coop[threadIdx.x >> 5], v};
-    coop_walk<kInd, false>(W, s, coop_lane(valid, sc, W, s), i, pi, scan, v);
+    coop_walk<kInd, false, kTailAll>(W, s, coop_lane(valid, sc, W, s), i, pi, scan, v);
     if (!valid) return;
     const uint32_t d = T.pofs[sc] + id[i];
     count_out[d] = v.count;
@@ -1560,13 +1726,20 @@ static WalkCtx global_ctx(const SortBuffers &B, const float4 *pos) {
 template <int kThreads>
 static void density_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel, float4 *rp,
                            float4 *fr, const NbrList &L, const RowWarps &RW, bool indirect,
-                           const uint32_t *status, cudaStream_t st) {
+                           uint32_t *deferred, uint32_t *status, cudaStream_t st) {
     // with row warps: at most n / 32 + rows warps (each row's last is partial)
     const uint32_t threads = launch_threads(T, RW);
-    if (indirect)
-        k_density<true, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, RW, status);
-    else
-        k_density<false, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(T, G, vel, rp, fr, L, RW, status);
+    if (indirect) {
+        k_density<true, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, RW, deferred, status);
+        k_density_deferred<true><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(T, G, vel, rp, fr, L,
+                                                                             deferred, status);
+    } else {
+        k_density<false, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, RW, deferred, status);
+        k_density_deferred<false><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(T, G, vel, rp, fr, L,
+                                                                              deferred, status);
+    }
 }
 
 cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
@@ -1582,8 +1755,9 @@ cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const floa
         RW = *rw;
     }
     if (T.n) {
-        if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, RW, indirect, B.status, st);
-        else density_launch<256>(T, G, vel, rp, fr, L, RW, indirect, B.status, st);
+        cudaMemsetAsync(B.status + kStatusDeferred, 0, 8, st);  // both deferred counts
+        if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
+        else density_launch<256>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
     }
     return cudaGetLastError();
 }
@@ -1592,13 +1766,18 @@ template <int kThreads>
 static void force_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel,
                          const float4 *rp, const float4 *fr, const NbrList &L, float4 *pos_out,
                          float4 *vel_out, float4 *force_out, bool indirect,
-                         const uint32_t *status, cudaStream_t st) {
-    if (indirect)
+                         uint32_t *deferred, uint32_t *status, cudaStream_t st) {
+    if (indirect) {
         k_force<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
-            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, status);
-    else
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+        k_force_deferred<true><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    } else {
         k_force<false, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
-            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, status);
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+        k_force_deferred<false><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    }
 }
 
 cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
@@ -1608,9 +1787,11 @@ cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4
     const WalkCtx G = global_ctx(B, pos);
     if (T.n) {
         if (threads == 128)
-            force_launch<128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect, B.status, st);
+            force_launch<128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
+                              B.deferred + T.n, B.status, st);
         else
-            force_launch<256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect, B.status, st);
+            force_launch<256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
+                              B.deferred + T.n, B.status, st);
     }
     return cudaGetLastError();
 }

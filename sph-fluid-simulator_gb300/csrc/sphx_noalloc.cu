@@ -16,7 +16,7 @@
 // Limits and sharing:
 //   * at most kMaxParticles (131,072) particles per call; more is rejected
 //     with SPHX_ERR_INVALID;
-//   * the array (about 6.5 MiB) lives in every GPU that loads the library
+//   * the array (about 7 MiB) lives in every GPU that loads the library
 //     until the process exits;
 //   * every call on a device uses the same array, which keeps the previous
 //     call's contents: the counts and status words are cleared at the start
@@ -56,7 +56,8 @@ constexpr size_t kOffTable = kOffStatus + 256;  // StepParams + particle / slot 
 constexpr size_t kOffRp = kOffTable + 1024;
 constexpr size_t kOffLarge = kOffRp + 16ull * kMaxParticles;  // queued large cells
 constexpr size_t kOffScat = kOffLarge + align256(8ull * (kMaxParticles / 64 + 2));
-constexpr size_t kScratchBytes = kOffScat + 8ull * kMaxParticles;
+constexpr size_t kOffDeferred = kOffScat + 8ull * kMaxParticles;
+constexpr size_t kScratchBytes = kOffDeferred + 4ull * kMaxParticles;
 static_assert(sizeof(sphx::StepParams) + 16 <= 1024, "scene table fits its scratch slot");
 
 static __device__ __align__(256) uint4 g_scratch[kScratchBytes / sizeof(uint4)];
@@ -145,6 +146,7 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     B.tile_sum = reinterpret_cast<uint32_t *>(base + kOffTiles);
     B.status = reinterpret_cast<uint32_t *>(base + kOffStatus);
     B.large = reinterpret_cast<uint2 *>(base + kOffLarge);
+    B.deferred = reinterpret_cast<uint32_t *>(base + kOffDeferred);
     B.large_cap = kMaxParticles / 64 + 2;
     B.slots = kSlots;
     B.max_cell = sphx::kLargeCell;

@@ -90,7 +90,7 @@ def brute_flags(cx, cy, cz, face_mask):
     return dup, faces
 
 
-def test_collision_flags_exact_dup_and_conservative_faces(sphx_lib):
+def test_collision_flags_exact(sphx_lib):
     L = sphx_lib.lib()
     rng = np.random.default_rng(0)
     # bucket collisions cluster near the origin (small products keep high bits
@@ -104,8 +104,7 @@ def test_collision_flags_exact_dup_and_conservative_faces(sphx_lib):
         fl = L.sphx_collision_flags(int(c[0]), int(c[1]), int(c[2]), 0x3F)
         assert bool(fl & 1) == dup
         for f in range(6):
-            if faces[f]:
-                assert (fl >> (1 + f)) & 1, (c, f)  # never misses a real collision
+            assert bool((fl >> (1 + f)) & 1) == faces[f], (c, f)
         ndup += dup
         nface += any(faces)
     assert ndup > 0 and nface > 0  # the sample exercises both cases
