@@ -171,7 +171,7 @@ Layout layout_for(size_t cn, size_t cs, size_t csc, size_t slots) {
                                         sizeof(sphx::StepParams) * csc, 4 * (csc + 1),
                                         4 * (csc + 1), 8ull * sphx::large_list_cap((uint32_t)cn),
                                         32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn,
-                                        4 * (csc + 1), 4 * (cs + 1), 8 * cn};
+                                        4 * (csc + 1), 4 * (cs + 1), 8 * cn + 4 * (cn / 32 + 1)};
     Layout L;
     size_t o = 0;
     for (int k = 0; k < Layout::kNum; ++k) {
@@ -460,9 +460,9 @@ int sphx::run_steps(sphx_handle *h, float dt, int nsteps) {
             cudaEvent_t *ev = &h->events[h->events_used];
             h->launches_per_step.resize(h->events.size() / 4);
             // sort 7, gather, row warps (1, 2 past 4095 rows), density and
-            // force with their deferred-particle companions
+            // its deferred particles, force over lists, walkers, deferred
             h->launches_per_step[h->events_used / 4] =
-                (reorder ? 12u : 11u) + (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
+                (reorder ? 13u : 12u) + (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
             h->events_used += 4;
             int pv = h->pv, idc = h->idc;
             SPHX_CUDA(enqueue_step(h, reorder, pv, idc, ev));

@@ -1345,60 +1345,89 @@ __device__ __forceinline__ void force_finish(const StepParams &P, const ForcePai
     vel_out[i] = v;
 }
 
-// Force of every particle: over its list when its neighbours fit one (same
-// neighbours, same order as the density walk), else by a warp-cooperative
-// walk over the neighbour records in that same order.  Only the lanes past
-// their list take part in the walk, the whole warp loading for them.
+// Force of every particle whose neighbours fit its list (same neighbours,
+// same order as the density walk), then integration and walls.  The others
+// are k_force_walk's, which this kernel tells which warps (32 cell-sorted
+// particles) hold one: keeping the walk out of this kernel leaves it 48
+// registers instead of 64 with spills (0.257 against 0.276 ms at 2.1M).
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads)
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
-            uint32_t *__restrict__ deferred, uint32_t *__restrict__ status) {
-    // particles past their list and off the cooperative path are listed in
-    // `deferred` for k_force_deferred
-    __shared__ RecordSmem<kInd> s_coop[kThreads / 32];
+            uint32_t *__restrict__ walk_warps, uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    // whole warps leave together: the cooperative walk needs every lane
-    if ((t & ~31u) >= T.n || (status[0] & kStatusErrorMask)) return;
-    const bool valid = t < T.n;
+    if (status[0] & kStatusErrorMask) return;
+    const bool valid = t < T.n;  // the grid is whole blocks: every lane gets here
     const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
-    const uint32_t sc = valid ? scene_of(T, i) : 0u;
+    const uint32_t cnt = valid ? L.count[i] : 0u;
+    const uint32_t wm = __ballot_sync(0xffffffffu, valid && cnt > L.slots);
+    if (wm && (threadIdx.x & 31u) == (uint32_t)(__ffs(wm) - 1))
+        walk_warps[atomicAdd(&status[kStatusWalkWarps], 1u)] = t >> 5;
+    if (!valid || cnt > L.slots) return;
+    const uint32_t sc = scene_of(T, i);
     const StepParams &P = T.params[sc];
     const float4 pi = G.pos[i];
     const float4 vi = vel[i];
     const float4 q = rp[i];
     ForcePair pair{vi, q.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const uint32_t cnt = valid ? L.count[i] : 0u;
-    if (cnt <= L.slots) {
-        // the row is 16-byte aligned (slots is a multiple of 4): four entries
-        // per load; entries past cnt in the last load are never used
-        const uint4 *row = reinterpret_cast<const uint4 *>(L.nbr + (size_t)i * L.slots);
+    // the row is 16-byte aligned (slots is a multiple of 4): four entries per
+    // load; entries past cnt in the last load are never used
+    const uint4 *row = reinterpret_cast<const uint4 *>(L.nbr + (size_t)i * L.slots);
 #pragma unroll 1
-        for (uint32_t k = 0; k < cnt; k += 4) {
-            const uint4 e = row[k >> 2];
-            const uint32_t left = cnt - k;
-            {  // two records in flight, then summed in list order
-                const uint32_t j1 = left > 1 ? e.y : e.x;
-                float4 a0, b0, a1, b1;
-                load_record(fr, e.x, a0, b0);
-                load_record(fr, j1, a1, b1);
-                pair_add_record(pair, a0, b0, pi);
-                if (left > 1) pair_add_record(pair, a1, b1, pi);
-            }
-            if (left > 2) {
-                const uint32_t j3 = left > 3 ? e.w : e.z;
-                float4 a2, b2, a3, b3;
-                load_record(fr, e.z, a2, b2);
-                load_record(fr, j3, a3, b3);
-                pair_add_record(pair, a2, b2, pi);
-                if (left > 3) pair_add_record(pair, a3, b3, pi);
-            }
+    for (uint32_t k = 0; k < cnt; k += 4) {
+        const uint4 e = row[k >> 2];
+        const uint32_t left = cnt - k;
+        {  // two records in flight, then summed in list order
+            const uint32_t j1 = left > 1 ? e.y : e.x;
+            float4 a0, b0, a1, b1;
+            load_record(fr, e.x, a0, b0);
+            load_record(fr, j1, a1, b1);
+            pair_add_record(pair, a0, b0, pi);
+            if (left > 1) pair_add_record(pair, a1, b1, pi);
+        }
+        if (left > 2) {
+            const uint32_t j3 = left > 3 ? e.w : e.z;
+            float4 a2, b2, a3, b3;
+            load_record(fr, e.z, a2, b2);
+            load_record(fr, j3, a3, b3);
+            pair_add_record(pair, a2, b2, pi);
+            if (left > 3) pair_add_record(pair, a3, b3, pi);
         }
     }
-    const bool walker = valid && cnt > L.slots;
-    bool mine = valid;
-    if (__any_sync(0xffffffffu, walker)) {
+    force_finish(P, pair, i, pi, vi, q.x, pos_out, vel_out, force_out);
+}
+
+// Force of the particles past their list (clumped fluid), over the warps
+// k_force listed: a warp-cooperative walk over the neighbour records in the
+// density walk's order, the whole warp loading for its walking lanes.
+// Walkers off the cooperative path (bucket collision, grid seam) are listed
+// in `deferred` for k_force_deferred.
+template <bool kInd, int kThreads>
+__global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads)
+    k_force_walk(SceneTable T, WalkCtx G, const float4 *__restrict__ vel,
+                 const float4 *__restrict__ rp, const float4 *__restrict__ fr, NbrList L,
+                 float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
+                 float4 *__restrict__ force_out, const uint32_t *__restrict__ walk_warps,
+                 uint32_t *__restrict__ deferred, uint32_t *__restrict__ status) {
+    __shared__ RecordSmem<kInd> s_coop[kThreads / 32];
+    if (status[0] & kStatusErrorMask) return;
+    // one warp per listed warp (the grid has one for every possible one):
+    // clumps make some walks far longer than others, and the hardware's block
+    // scheduling balances them
+    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (q >= status[kStatusWalkWarps]) return;
+    {
+        const uint32_t t = walk_warps[q] * 32u + lane;
+        const bool valid = t < T.n;
+        const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
+        const bool walker = valid && L.count[i] > L.slots;
+        const uint32_t sc = valid ? scene_of(T, i) : 0u;
+        const StepParams &P = T.params[sc];
+        const float4 pi = G.pos[i];
+        const float4 vi = vel[i];
+        const float4 r = rp[i];
+        ForcePair pair{vi, r.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const WalkCtx W = walk_ctx(T, G, sc, P, status);
         WalkStart s;
         walk_start(P, pi, s);
@@ -1407,9 +1436,8 @@ __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads
         const CoopLane cl = coop_lane(walker, sc, W, s);
         defer_lanes(walker && !cl.fast, t, deferred, &status[kStatusDeferredForce]);
         coop_walk<kInd, true, kTailNone>(W, s, cl, i, pi, scan, v);
-        mine = valid && (!walker || cl.fast);
+        if (cl.fast) force_finish(P, pair, i, pi, vi, r.x, pos_out, vel_out, force_out);
     }
-    if (mine) force_finish(P, pair, i, pi, vi, q.x, pos_out, vel_out, force_out);
 }
 
 // The particles k_force deferred, one warp each (warp_walk over the
@@ -1755,7 +1783,8 @@ cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const floa
         RW = *rw;
     }
     if (T.n) {
-        cudaMemsetAsync(B.status + kStatusDeferred, 0, 8, st);  // both deferred counts
+        // both deferred counts and the walker warps' count
+        cudaMemsetAsync(B.status + kStatusDeferred, 0, 12, st);
         if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
         else density_launch<256>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
     }
@@ -1766,15 +1795,21 @@ template <int kThreads>
 static void force_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel,
                          const float4 *rp, const float4 *fr, const NbrList &L, float4 *pos_out,
                          float4 *vel_out, float4 *force_out, bool indirect,
-                         uint32_t *deferred, uint32_t *status, cudaStream_t st) {
+                         uint32_t *deferred, uint32_t *walk_warps, uint32_t *status,
+                         cudaStream_t st) {
+    const unsigned walk_blocks = blocks(T.n, kThreads);
     if (indirect) {
         k_force<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
-            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);
+        k_force_walk<true, kThreads><<<walk_blocks, kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, deferred, status);
         k_force_deferred<true><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
             T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
     } else {
         k_force<false, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
-            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);
+        k_force_walk<false, kThreads><<<walk_blocks, kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, deferred, status);
         k_force_deferred<false><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
             T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
     }
@@ -1788,10 +1823,10 @@ cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4
     if (T.n) {
         if (threads == 128)
             force_launch<128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
-                              B.deferred + T.n, B.status, st);
+                              B.deferred + T.n, B.deferred + 2 * (size_t)T.n, B.status, st);
         else
             force_launch<256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
-                              B.deferred + T.n, B.status, st);
+                              B.deferred + T.n, B.deferred + 2 * (size_t)T.n, B.status, st);
     }
     return cudaGetLastError();
 }

@@ -22,8 +22,9 @@ struct SortBuffers {
     uint32_t *tile_sum;  // ceil((slots + 1) / 4096)
     uint32_t *status;    // 2 words: error bits, x-wrap flag (see below)
     uint2 *large;        // cells longer than 64 queued for the block sort
-    uint32_t *deferred;  // 2n: cell-sorted positions of the particles the density
-                         // pass (first n) and the force pass (last n) defer
+    uint32_t *deferred;  // 2n + n / 32 + 1: cell-sorted positions of the particles the
+                         // density pass (first n) and the force pass (next n) defer,
+                         // then the warps of the force pass that hold a walker
     uint32_t large_cap;  // entries of `large` (n / 64 + 2 suffices)
     uint32_t slots;      // gx * gy * gz
     uint32_t max_cell;   // occupancy above which a step refuses to walk (<= kLargeCell)
@@ -43,9 +44,11 @@ constexpr uint32_t kStatusOverflowBit = 2u;  // a cell above max_cell
 constexpr uint32_t kStatusErrorMask = 3u;
 // status[3]: first rejected row of an upload; status[4], status[5]:
 // particles the density and force passes deferred to their per-particle
-// companions (both cleared before the density pass).
+// companions; status[6]: warps of the force pass that hold a walker (all
+// three cleared before the density pass).
 constexpr uint32_t kStatusDeferred = 4u;
 constexpr uint32_t kStatusDeferredForce = 5u;
+constexpr uint32_t kStatusWalkWarps = 6u;
 
 cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                         cudaStream_t st);
