@@ -202,14 +202,16 @@ def test_against_fp64_oracle(sphx_lib, port):
         assert e_gpu < REL_TOL and e_gpu <= max(2 * e_ref, 1e-6)
 
 
-@pytest.mark.parametrize("R", [1, 4])
-def test_aliased_tiny_grid_is_exact(sphx_lib, port, R):
-    """A 5x5x5 cell grid far smaller than the scene: slots alias, results don't change."""
+@pytest.mark.parametrize("R,slots", [(1, 256), (4, 256), (1, 1), (4, 1)])
+def test_aliased_tiny_grid_is_exact(sphx_lib, port, R, slots):
+    """A 5x5x5 cell grid far smaller than the scene: slots alias, results don't
+    change.  Two of its five x columns are the grid's seam, whose particles
+    walk alone; with a one-entry list they walk in the force pass too."""
     pos, box = sphx_lib.dambreak(16, box_dims=(2.0, 2.0, 2.0), seed=4)
     vel = np.random.default_rng(3).normal(0, 0.5, pos.shape).astype(np.float32)
     r = port.step(pos, vel, CONFIG_ARGS, 0.002, box=box.as_array()).by_id()
     with scene(sphx_lib, CONFIG_ARGS, pos, vel, box=box, grid_dims=(5, 5, 5),
-               grid_origin=(-3, 0, 2), reorder_interval=R) as sc:
+               grid_origin=(-3, 0, 2), reorder_interval=R, neighbor_slots=slots) as sc:
         cnt, dig = sc.neighbor_digest()
         sc.step(0.002, 1)
         out = sc.read()
@@ -217,6 +219,21 @@ def test_aliased_tiny_grid_is_exact(sphx_lib, port, R):
     assert np.array_equal(cnt, c2) and np.array_equal(dig, d2)
     for f in ("rho", "prs", "force", "pos", "vel"):
         assert rel_err(out[f], getattr(r, f)) < REL_TOL, f
+
+
+def test_aliased_tiny_grid_list_and_walk_agree(sphx_lib):
+    """On the aliased grid the seam particles' force comes from their list or
+    from the walk of the force pass's deferred particles: the same bits."""
+    pos, box = sphx_lib.dambreak(16, box_dims=(2.0, 2.0, 2.0), seed=4)
+    vel = np.random.default_rng(3).normal(0, 0.5, pos.shape).astype(np.float32)
+    outs = []
+    for slots in (1, 1024):
+        with scene(sphx_lib, CONFIG_ARGS, pos, vel, box=box, grid_dims=(5, 5, 5),
+                   grid_origin=(-3, 0, 2), neighbor_slots=slots) as sc:
+            sc.step(0.002, 3)
+            outs.append(sc.read())
+    for f in ("rho", "prs", "force", "pos", "vel"):
+        assert np.array_equal(outs[0][f], outs[1][f]), f
 
 
 def test_dense_collision_region_digest(sphx_lib, port):
