@@ -157,7 +157,7 @@ struct Layout {
     enum {
         kPos0, kPos1, kVel0, kVel1, kId0, kId1, kRp, kForce, kKey, kRank, kOrder, kCount,
         kStart, kTiles, kStatus, kStaging, kParams, kPofs, kSofs, kLarge, kFr, kNbr, kNcount,
-        kScat, kRofs, kRowOfs, kDeferred, kNum
+        kScat, kRofs, kRowOfs, kDeferred, kCflags, kNum
     };
     size_t off[kNum];
     size_t total;
@@ -171,7 +171,8 @@ Layout layout_for(size_t cn, size_t cs, size_t csc, size_t slots) {
                                         sizeof(sphx::StepParams) * csc, 4 * (csc + 1),
                                         4 * (csc + 1), 8ull * sphx::large_list_cap((uint32_t)cn),
                                         32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn,
-                                        4 * (csc + 1), 4 * (cs + 1), 8 * cn + 4 * (cn / 32 + 1)};
+                                        4 * (csc + 1), 4 * (cs + 1), 8 * cn + 4 * (cn / 32 + 1),
+                                        cs + 1};
     Layout L;
     size_t o = 0;
     for (int k = 0; k < Layout::kNum; ++k) {
@@ -206,6 +207,7 @@ void bind(sphx_handle *h, char *a, const Layout &L) {
     h->d_sofs = (uint32_t *)(a + L.off[Layout::kSofs]);
     h->sb.large = (uint2 *)(a + L.off[Layout::kLarge]);
     h->sb.deferred = (uint32_t *)(a + L.off[Layout::kDeferred]);
+    h->sb.cflags = (const uint8_t *)(a + L.off[Layout::kCflags]);
     h->fr = (float4 *)(a + L.off[Layout::kFr]);
     h->nbr = (uint32_t *)(a + L.off[Layout::kNbr]);
     h->ncount = (uint32_t *)(a + L.off[Layout::kNcount]);
@@ -254,7 +256,12 @@ int upload_tables(sphx_handle *h) {
     h->sb.slots = h->slots;
     h->params_valid = false;
     // every readout reads the constants (h, walls) from the device table
-    return sphx::ensure_params(h, h->params_dt);
+    const int rc = sphx::ensure_params(h, h->params_dt);
+    if (rc != SPHX_OK) return rc;
+    // the grids' cell flags, after the constants they are computed from
+    SPHX_CUDA(sphx::launch_cell_flags(sphx::table_of(h), h->slots,
+                                      const_cast<uint8_t *>(h->sb.cflags), h->stream));
+    return SPHX_OK;
 }
 
 // Uploads one scene's host state into rows [first, first + n) of buffer

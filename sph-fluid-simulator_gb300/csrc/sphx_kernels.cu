@@ -327,6 +327,7 @@ struct WalkCtx {
     float h;
     float h2w;  // h^2 (1 + 2^-18): squared half-width bound of the row windows
     bool xmono;  // every particle inside the grid's x extent this step
+    const uint8_t *__restrict__ cflags;  // this scene's cell flags (k_cell_flags), or NULL
 };
 
 // One run of cell-sorted slots [a, b): every particle j != self with
@@ -551,13 +552,39 @@ struct WalkStart {
     uint32_t flags;
 };
 
-__device__ __forceinline__ bool walk_start(const StepParams &P, float4 pi, WalkStart &s) {
+// The flags come from the scene's cell-flag table when the particle's cell
+// is the one its slot was computed for (the grid's own extent), else they
+// are computed here.
+__device__ __forceinline__ bool walk_start(const WalkCtx &W, const StepParams &P, float4 pi,
+                                           WalkStart &s) {
     s.c = cell_pos(pi, P.h);
-    slot_of(P.grid, s.c.cx, s.c.cy, s.c.cz, s.mx, s.my, s.mz);
+    const uint32_t k = slot_of(P.grid, s.c.cx, s.c.cy, s.c.cz, s.mx, s.my, s.mz);
     const uint32_t near = near_faces_1d(s.c.qx, s.c.cx) | (near_faces_1d(s.c.qy, s.c.cy) << 2) |
                           (near_faces_1d(s.c.qz, s.c.cz) << 4);
-    s.flags = collision_flags(s.c.cx, s.c.cy, s.c.cz, near);
+    const bool own = (uint32_t)s.c.cx - (uint32_t)P.grid.ox == (uint32_t)s.mx &&
+                     (uint32_t)s.c.cy - (uint32_t)P.grid.oy == (uint32_t)s.my &&
+                     (uint32_t)s.c.cz - (uint32_t)P.grid.oz == (uint32_t)s.mz;
+    if (W.cflags && own)
+        s.flags = W.cflags[k] & (kFlagDup | (near << kFlagFaceShift));
+    else
+        s.flags = collision_flags(s.c.cx, s.c.cy, s.c.cz, near);
     return s.flags == 0u;
+}
+
+// Collision flags of every slot's own cell (all six faces), once per grid.
+__global__ void k_cell_flags(SceneTable T, uint32_t slots, uint8_t *__restrict__ cflags) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= slots) return;
+    uint32_t lo = 0, hi = T.nscenes;  // scene: the last s with sofs[s] <= k
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (T.sofs[mid] <= k) lo = mid;
+        else hi = mid;
+    }
+    const Grid &g = T.params[lo].grid;
+    const uint32_t l = k - T.sofs[lo], gx = (uint32_t)g.gx, gy = (uint32_t)g.gy;
+    const int mx = (int)(l % gx), my = (int)((l / gx) % gy), mz = (int)(l / (gx * gy));
+    cflags[k] = (uint8_t)collision_flags(mx + g.ox, my + g.oy, mz + g.oz, 0x3Fu);
 }
 
 template <bool kInd, class V>
@@ -1032,6 +1059,7 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
                                             const StepParams &P, const uint32_t *status) {
     WalkCtx W = G;
     W.start = G.start + T.sofs[sc];
+    if (G.cflags) W.cflags = G.cflags + T.sofs[sc];
     W.grid = P.grid;
     W.h2 = P.h2;
     W.h = P.h;
@@ -1103,7 +1131,7 @@ __global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThrea
     const WalkCtx W = walk_ctx(T, G, sc, P, status);
     const float4 pi = W.pos[i];
     WalkStart s;
-    walk_start(P, pi, s);
+    walk_start(W, P, pi, s);
     const bool slow = valid && s.flags != 0u;
     defer_lanes(slow, t, deferred, &status[kStatusDeferred]);
     DensityVisitor v{P.h2, 0.f, 0.f, valid && !slow ? density_row(W, s, L, i) : nullptr, L.slots, 0u};
@@ -1132,7 +1160,7 @@ __global__ void __launch_bounds__(kDeferredThreads)
         const WalkCtx W = walk_ctx(T, G, sc, P, status);
         const float4 pi = W.pos[i];
         WalkStart s;
-        walk_start(P, pi, s);
+        walk_start(W, P, pi, s);
         DensityVisitor v{P.h2, 0.f, 0.f, lane == 0 ? density_row(W, s, L, i) : nullptr, L.slots, 0u};
         PosScan<kInd, DensityVisitor> scan{s_chunk[threadIdx.x >> 5], v};
         warp_walk<kInd>(W, s, i, pi, scan);
@@ -1430,7 +1458,7 @@ __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads
         ForcePair pair{vi, r.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         const WalkCtx W = walk_ctx(T, G, sc, P, status);
         WalkStart s;
-        walk_start(P, pi, s);
+        walk_start(W, P, pi, s);
         RecordScan<kInd> scan{s_coop[threadIdx.x >> 5], fr, pair};
         ForceVisitor v{pair, fr, pi};
         const CoopLane cl = coop_lane(walker, sc, W, s);
@@ -1465,7 +1493,7 @@ __global__ void __launch_bounds__(kDeferredThreads)
         const float4 r = rp[i];
         ForcePair pair{vi, r.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         WalkStart s;
-        walk_start(P, pi, s);
+        walk_start(W, P, pi, s);
         RecordScan<kInd> scan{s_chunk[threadIdx.x >> 5], fr, pair};
         warp_walk<kInd>(W, s, i, pi, scan);
         if (lane == 0) force_finish(P, pair, i, pi, vi, r.x, pos_out, vel_out, force_out);
@@ -1508,7 +1536,7 @@ __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ i
     const WalkCtx W = walk_ctx(T, G, sc, P, status);
     const float4 pi = W.pos[i];
     WalkStart s;
-    walk_start(P, pi, s);
+    walk_start(W, P, pi, s);
     DigestVisitor v{id, 0u, 0ull, 0u};
     // the same walk as k_density's
     __shared__ PosSmem<kInd> s_coop[kDigestThreads / 32];
@@ -1729,6 +1757,12 @@ cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 
     return cudaGetLastError();
 }
 
+cudaError_t launch_cell_flags(const SceneTable &T, uint32_t slots, uint8_t *cflags,
+                              cudaStream_t st) {
+    if (slots) k_cell_flags<<<blocks(slots, 256), 256, 0, st>>>(T, slots, cflags);
+    return cudaGetLastError();
+}
+
 cudaError_t prepare_device() {
     return cudaFuncSetAttribute(k_cellsort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 8 * kLargeCell);
@@ -1748,6 +1782,7 @@ static WalkCtx global_ctx(const SortBuffers &B, const float4 *pos) {
     W.order = B.order;
     W.start = B.start;
     W.xmono = true;
+    W.cflags = B.cflags;
     return W;
 }
 

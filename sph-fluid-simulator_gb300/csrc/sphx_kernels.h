@@ -22,6 +22,7 @@ struct SortBuffers {
     uint32_t *tile_sum;  // ceil((slots + 1) / 4096)
     uint32_t *status;    // 2 words: error bits, x-wrap flag (see below)
     uint2 *large;        // cells longer than 64 queued for the block sort
+    const uint8_t *cflags;  // slots: collision flags of each slot's own cell, or NULL
     uint32_t *deferred;  // 2n + n / 32 + 1: cell-sorted positions of the particles the
                          // density pass (first n) and the force pass (next n) defer,
                          // then the warps of the force pass that hold a walker
@@ -52,6 +53,10 @@ constexpr uint32_t kStatusWalkWarps = 6u;
 
 cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                         cudaStream_t st);
+// The collision flags (dup bit, six exact face bits) of every slot's own
+// cell, for the walks' lookup; once per change of the scenes' grids.
+cudaError_t launch_cell_flags(const SceneTable &T, uint32_t slots, uint8_t *cflags,
+                              cudaStream_t st);
 // Once per device before the first launch_sort (outside any stream capture):
 // allows the large-cell sort its shared memory.
 cudaError_t prepare_device();

@@ -147,6 +147,7 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     B.status = reinterpret_cast<uint32_t *>(base + kOffStatus);
     B.large = reinterpret_cast<uint2 *>(base + kOffLarge);
     B.deferred = reinterpret_cast<uint32_t *>(base + kOffDeferred);
+    B.cflags = nullptr;  // the walks compute the flags
     B.large_cap = kMaxParticles / 64 + 2;
     B.slots = kSlots;
     B.max_cell = sphx::kLargeCell;
