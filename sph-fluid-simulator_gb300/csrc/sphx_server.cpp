@@ -44,11 +44,13 @@ struct Request {
 // arena plus its cell-grid slots (counts and starts), as laid out by
 // sphx_api.cpp, with the grid estimated from the particle count.
 size_t footprint(uint32_t n) {
-    // state, ids, records, sort scratch, staging, neighbour records and lists
+    // state, ids, records, sort scratch, staging, neighbour records and lists,
+    // deferred-particle lists
     const size_t per_particle =
-        16 * 4 + 4 * 2 + 16 + 16 + 4 * 3 + 8 + 24 + 32 + 4 * sphx::kNbrSlotsDefault + 4 + 1;
+        16 * 4 + 4 * 2 + 16 + 16 + 4 * 3 + 8 + 24 + 32 + 4 * sphx::kNbrSlotsDefault + 4 + 9;
+    // counts, starts, row offsets (at most one per slot), cell flags
     const size_t slots = 16ull * n + 4096;
-    return per_particle * n + 8 * slots + 4096;
+    return per_particle * n + 13 * slots + 4096;
 }
 
 }  // namespace
