@@ -1440,12 +1440,17 @@ __global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads
                  uint32_t *__restrict__ deferred, uint32_t *__restrict__ status) {
     __shared__ RecordSmem<kInd> s_coop[kThreads / 32];
     if (status[0] & kStatusErrorMask) return;
-    // one warp per listed warp (the grid has one for every possible one):
-    // clumps make some walks far longer than others, and the hardware's block
-    // scheduling balances them
-    const uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
-    if (q >= status[kStatusWalkWarps]) return;
-    {
+    // each warp takes the next listed warp until none is left: clumps make
+    // some walks far longer than others, so the work is handed out as it
+    // goes; warps past the list's length have nothing to take
+    const uint32_t m = status[kStatusWalkWarps], lane = threadIdx.x & 31u;
+    if (((blockIdx.x * blockDim.x + threadIdx.x) >> 5) >= m) return;
+#pragma unroll 1
+    for (;;) {
+        uint32_t q = 0;
+        if (lane == 0) q = atomicAdd(&status[kStatusWalkNext], 1u);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= m) break;
         const uint32_t t = walk_warps[q] * 32u + lane;
         const bool valid = t < T.n;
         const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
@@ -1818,8 +1823,8 @@ cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const floa
         RW = *rw;
     }
     if (T.n) {
-        // both deferred counts and the walker warps' count
-        cudaMemsetAsync(B.status + kStatusDeferred, 0, 12, st);
+        // both deferred counts, the walker warps' count and their next one
+        cudaMemsetAsync(B.status + kStatusDeferred, 0, 16, st);
         if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
         else density_launch<256>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
     }
@@ -1832,7 +1837,9 @@ static void force_launch(const SceneTable &T, const WalkCtx &G, const float4 *ve
                          float4 *vel_out, float4 *force_out, bool indirect,
                          uint32_t *deferred, uint32_t *walk_warps, uint32_t *status,
                          cudaStream_t st) {
-    const unsigned walk_blocks = blocks(T.n, kThreads);
+    // the walkers' kernel: as many warps as the GPU holds at once (or fewer)
+    const unsigned walk_blocks =
+        std::min<unsigned>(blocks(T.n, kThreads), 152u * (SPHX_FORCE_THREADS_PER_SM / kThreads));
     if (indirect) {
         k_force<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
             T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);

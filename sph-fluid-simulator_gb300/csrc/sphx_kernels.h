@@ -45,11 +45,13 @@ constexpr uint32_t kStatusOverflowBit = 2u;  // a cell above max_cell
 constexpr uint32_t kStatusErrorMask = 3u;
 // status[3]: first rejected row of an upload; status[4], status[5]:
 // particles the density and force passes deferred to their per-particle
-// companions; status[6]: warps of the force pass that hold a walker (all
-// three cleared before the density pass).
+// companions; status[6]: warps of the force pass that hold a walker;
+// status[7]: the next of those the walkers' kernel hands out (all four
+// cleared before the density pass).
 constexpr uint32_t kStatusDeferred = 4u;
 constexpr uint32_t kStatusDeferredForce = 5u;
 constexpr uint32_t kStatusWalkWarps = 6u;
+constexpr uint32_t kStatusWalkNext = 7u;
 
 cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                         cudaStream_t st);
