@@ -35,6 +35,9 @@
 #ifndef SPHX_DENSITY_THREADS_PER_SM
 #define SPHX_DENSITY_THREADS_PER_SM 1024
 #endif
+#ifndef SPHX_FORCE_LIST_THREADS_PER_SM
+#define SPHX_FORCE_LIST_THREADS_PER_SM 1024
+#endif
 #ifndef SPHX_FORCE_THREADS_PER_SM
 #define SPHX_FORCE_THREADS_PER_SM 1024
 #endif
@@ -242,7 +245,7 @@ __global__ void k_cellsort(uint32_t n, const float4 *__restrict__ pos,
         }
         return;
     }
-    const float xi = pos[i].x;
+    const float xi = __uint_as_float(scat[a + rank[i]].y);  // k_scatter's copy of x
     uint32_t r = 0;
 #pragma unroll 4
     for (uint32_t t = a; t < a + c; ++t) {
@@ -1379,7 +1382,7 @@ __device__ __forceinline__ void force_finish(const StepParams &P, const ForcePai
 // particles) hold one: keeping the walk out of this kernel leaves it 48
 // registers instead of 64 with spills (0.257 against 0.276 ms at 2.1M).
 template <bool kInd, int kThreads>
-__global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads)
+__global__ void __launch_bounds__(kThreads, SPHX_FORCE_LIST_THREADS_PER_SM / kThreads)
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
