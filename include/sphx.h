@@ -119,8 +119,8 @@ typedef struct sphx_device_view {
  * on the handle's stream). */
 typedef struct sphx_kernel_times {
     double sort_ms;    /* keys + scan + scatter + cell sort + reorder */
-    double density_ms; /* k_density */
-    double force_ms;   /* k_force (force + integrate + walls) */
+    double density_ms; /* row warps + density (+ its deferred particles) */
+    double force_ms;   /* force over lists, walkers, deferred (+ integrate, walls) */
     uint64_t steps;
     uint64_t launches; /* kernels launched by those steps */
 } sphx_kernel_times;
@@ -144,7 +144,7 @@ void sphx_cell(float x, float y, float z, float h, int32_t out[3]);
 /* Bucket-collision flags of the 27 cells around a cell (host evaluation of
  * the test the kernels use): bit 0 = two neighbour cells share a bucket;
  * bit 1+f = a cell two away across face f (-x,+x,-y,+y,-z,+z, only faces in
- * face_mask) may share a visited bucket. */
+ * face_mask) shares a visited bucket.  Both bits are exact. */
 uint32_t sphx_collision_flags(int32_t cx, int32_t cy, int32_t cz, uint32_t face_mask);
 
 /* Fills 3*nx*ny*nz floats. */
