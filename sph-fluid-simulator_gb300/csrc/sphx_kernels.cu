@@ -229,8 +229,7 @@ __global__ void k_scatter(uint32_t n, const float4 *__restrict__ pos,
 // that arrived first, for k_cellsort_large instead.
 constexpr uint32_t kSmallCell = 64;
 
-__global__ void k_cellsort(uint32_t n, const float4 *__restrict__ pos,
-                           const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
+__global__ void k_cellsort(uint32_t n, const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
                            const uint32_t *__restrict__ start, const uint2 *__restrict__ scat,
                            uint32_t *__restrict__ order, uint32_t *__restrict__ status,
                            uint2 *__restrict__ large, uint32_t large_cap) {
@@ -1757,7 +1756,7 @@ cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 
     k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.start);
     if (n) {
         k_scatter<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.scat, B.status);
-        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.scat, B.order,
+        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, B.key, B.rank, B.start, B.scat, B.order,
                                                  B.status, B.large, B.large_cap);
         k_cellsort_large<<<kLargeBlocks, 512, 8 * kLargeCell, st>>>(B.scat, B.order, B.status,
                                                                     B.large, B.large_cap);
