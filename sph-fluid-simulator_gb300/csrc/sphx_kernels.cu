@@ -47,9 +47,11 @@ namespace {
 
 __device__ __forceinline__ uint32_t slot_of(const Grid &g, int cx, int cy, int cz, int &mx,
                                             int &my, int &mz) {
-    mx = wrap_mod(cx - g.ox, g.gx);
-    my = wrap_mod(cy - g.oy, g.gy);
-    mz = wrap_mod(cz - g.oz, g.gz);
+    // inside the grid's extent (almost always) the modulo is the identity
+    const int dx = cx - g.ox, dy = cy - g.oy, dz = cz - g.oz;
+    mx = (unsigned)dx < (unsigned)g.gx ? dx : wrap_mod(dx, g.gx);
+    my = (unsigned)dy < (unsigned)g.gy ? dy : wrap_mod(dy, g.gy);
+    mz = (unsigned)dz < (unsigned)g.gz ? dz : wrap_mod(dz, g.gz);
     return ((uint32_t)mz * (uint32_t)g.gy + (uint32_t)my) * (uint32_t)g.gx + (uint32_t)mx;
 }
 
