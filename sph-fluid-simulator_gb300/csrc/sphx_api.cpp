@@ -466,10 +466,13 @@ int sphx::run_steps(sphx_handle *h, float dt, int nsteps) {
             }
             cudaEvent_t *ev = &h->events[h->events_used];
             h->launches_per_step.resize(h->events.size() / 4);
-            // sort 7, gather, row warps (1, 2 past 4095 rows), density and
-            // its deferred particles, force over lists, walkers, deferred
+            // sort 6 (7 past 1024 scan tiles), gather, row warps (1, 2 past
+            // 4095 rows), density and its deferred particles, force over
+            // lists, walkers, deferred
+            const uint32_t tiles = (h->slots + 1u + 4095u) / 4096u;
             h->launches_per_step[h->events_used / 4] =
-                (reorder ? 13u : 12u) + (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
+                (reorder ? 12u : 11u) + (tiles > 1024u) +
+                (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
             h->events_used += 4;
             int pv = h->pv, idc = h->idc;
             SPHX_CUDA(enqueue_step(h, reorder, pv, idc, ev));

@@ -162,7 +162,8 @@ __global__ void k_scan_tiles(const uint32_t *__restrict__ count, uint32_t m,
     if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
 }
 
-// Single block: exclusive scan of the tile sums in place.
+// Single block: exclusive scan of the tile sums in place (grids of more
+// than kSelfPrefixTiles tiles).
 __global__ void k_scan_tile_sums(uint32_t *__restrict__ tile_sum, uint32_t ntiles) {
     uint32_t carry = 0;
     for (uint32_t base = 0; base < ntiles; base += kScanTile) {
@@ -187,10 +188,26 @@ __global__ void k_scan_tile_sums(uint32_t *__restrict__ tile_sum, uint32_t ntile
 }
 
 // cellStart[i] = exclusive prefix of count[i]; count is cleared for the next
-// step in the same pass.
+// step in the same pass.  The tile's offset: with kSelfPrefix the sum of the
+// earlier tiles' totals, added up by one warp (up to kSelfPrefixTiles tiles,
+// which saves the pass over the tile sums), else tile_sum already holds it.
+constexpr uint32_t kSelfPrefixTiles = 1024;
+template <bool kSelfPrefix>
 __global__ void k_scan_apply(uint32_t *__restrict__ count, uint32_t m,
-                             const uint32_t *__restrict__ tile_prefix,
+                             const uint32_t *__restrict__ tile_sum,
                              uint32_t *__restrict__ start) {
+    __shared__ uint32_t s_prefix;
+    if (threadIdx.x < 32) {
+        uint32_t p = 0;
+        if (kSelfPrefix) {
+            for (uint32_t b = threadIdx.x; b < blockIdx.x; b += 32) p += tile_sum[b];
+#pragma unroll
+            for (int d = 16; d; d >>= 1) p += __shfl_xor_sync(0xffffffffu, p, d);
+        } else {
+            p = tile_sum[blockIdx.x];
+        }
+        if (threadIdx.x == 0) s_prefix = p;
+    }
     const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     uint32_t s = 0;
@@ -200,8 +217,8 @@ __global__ void k_scan_apply(uint32_t *__restrict__ count, uint32_t m,
         s += v[k];
     }
     uint32_t excl;
-    block_exclusive_scan(s, excl);
-    uint32_t run = tile_prefix[blockIdx.x] + excl;
+    block_exclusive_scan(s, excl);  // its barriers also publish s_prefix
+    uint32_t run = s_prefix + excl;
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         if (base + k < m) {
@@ -214,12 +231,17 @@ __global__ void k_scan_apply(uint32_t *__restrict__ count, uint32_t m,
 
 // Each cell's run in arrival order: (particle, x bits) pairs.
 __global__ void k_scatter(uint32_t n, const float4 *__restrict__ pos,
-                          const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
+                          uint32_t *__restrict__ key, uint32_t *__restrict__ rank,
                           const uint32_t *__restrict__ start, uint2 *__restrict__ scat,
                           const uint32_t *__restrict__ status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (*status & kStatusOverflowBit)) return;
-    scat[start[key[i]] + rank[i]] = make_uint2(i, __float_as_uint(pos[i].x));
+    const uint32_t k = key[i], a = start[k], c = start[k + 1] - a, r = rank[i];
+    scat[a + r] = make_uint2(i, __float_as_uint(pos[i].x));
+    // for the cell sort: the cell's run and the place in it (c <= max_cell
+    // <= kLargeCell < 2^16 without an overflow)
+    key[i] = a;
+    rank[i] = r | (c << 16);
 }
 
 // Each particle's place in its cell's run sorted by (x, particle index): the
@@ -231,22 +253,22 @@ __global__ void k_scatter(uint32_t n, const float4 *__restrict__ pos,
 // that arrived first, for k_cellsort_large instead.
 constexpr uint32_t kSmallCell = 64;
 
-__global__ void k_cellsort(uint32_t n, const uint32_t *__restrict__ key, const uint32_t *__restrict__ rank,
-                           const uint32_t *__restrict__ start, const uint2 *__restrict__ scat,
+__global__ void k_cellsort(uint32_t n, const uint32_t *__restrict__ key,
+                           const uint32_t *__restrict__ rank, const uint2 *__restrict__ scat,
                            uint32_t *__restrict__ order, uint32_t *__restrict__ status,
                            uint2 *__restrict__ large, uint32_t large_cap) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || (status[0] & kStatusErrorMask)) return;
-    const uint32_t k = key[i];
-    const uint32_t a = start[k], c = start[k + 1] - a;
+    // k_scatter left the cell's run start in key and (place | count << 16) in rank
+    const uint32_t a = key[i], rc = rank[i], c = rc >> 16, place = rc & 0xFFFFu;
     if (c > kSmallCell) {
-        if (rank[i] == 0u) {
+        if (place == 0u) {
             const uint32_t slot = atomicAdd(&status[2], 1u);
             if (slot < large_cap) large[slot] = make_uint2(a, c);
         }
         return;
     }
-    const float xi = __uint_as_float(scat[a + rank[i]].y);  // k_scatter's copy of x
+    const float xi = __uint_as_float(scat[a + place].y);  // k_scatter's copy of x
     uint32_t r = 0;
 #pragma unroll 4
     for (uint32_t t = a; t < a + c; ++t) {
@@ -1754,11 +1776,15 @@ cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 
     cudaMemsetAsync(B.status + 1, 0, 8, st);  // x-wrap flag, large-cell count
     if (n) k_keys<<<blocks(n, bs), bs, 0, st>>>(T, pos, B.key, B.rank, B.count, B.status);
     k_scan_tiles<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.max_cell, B.status);
-    k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(B.tile_sum, ntiles);
-    k_scan_apply<<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.start);
+    if (ntiles <= kSelfPrefixTiles) {
+        k_scan_apply<true><<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.start);
+    } else {
+        k_scan_tile_sums<<<1, kScanThreads, 0, st>>>(B.tile_sum, ntiles);
+        k_scan_apply<false><<<ntiles, kScanThreads, 0, st>>>(B.count, m, B.tile_sum, B.start);
+    }
     if (n) {
         k_scatter<<<blocks(n, bs), bs, 0, st>>>(n, pos, B.key, B.rank, B.start, B.scat, B.status);
-        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, B.key, B.rank, B.start, B.scat, B.order,
+        k_cellsort<<<blocks(n, bs), bs, 0, st>>>(n, B.key, B.rank, B.scat, B.order,
                                                  B.status, B.large, B.large_cap);
         k_cellsort_large<<<kLargeBlocks, 512, 8 * kLargeCell, st>>>(B.scat, B.order, B.status,
                                                                     B.large, B.large_cap);
