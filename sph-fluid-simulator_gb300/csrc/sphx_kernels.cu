@@ -10,9 +10,16 @@
 //                 every float sum) is deterministic (k_cellsort_large: cells
 //                 of more than 64 particles)
 //   k_gather      every R steps: permute pos/vel/id into cell order
-//   k_density     poly6 density and pressure            (sph.cpp:28-76)
-//   k_force       spiky pressure + viscosity force, then integration and
-//                 damped wall reflection                 (sph.cpp:80-181)
+//   k_row_warps   the density pass's warps, one cell row each
+//   k_density     poly6 density and pressure            (sph.cpp:28-76),
+//                 the neighbour lists and records for the force pass
+//                 (k_density_deferred: particles with a bucket collision)
+//   k_force       spiky pressure + viscosity force over the lists, then
+//                 integration and damped wall reflection (sph.cpp:80-181)
+//                 (k_force_walk: particles past their list; k_force_deferred:
+//                 those of them off the cooperative walk)
+//
+// Once per grid, k_cell_flags tabulates every slot's collision flags.
 //
 // The neighbour walk visits the 27 cells around a particle's cell through the
 // grid (x-adjacent cells are adjacent slots, so each of the 9 (dy, dz) rows is
