@@ -327,25 +327,27 @@ def run_steps_only(a):
 
 
 def run_reference(a):
+    """The reference arm: the CPU restatement alone, on the same workload.
+    Its inputs come from the oracle's numpy generators (bit-identical to the
+    product's), so this arm loads nothing of the product."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    pos, box, s = workload()
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
     port = pyoracle.Port()
-    import sphx
-    args = sphx.args_array(s)
+    pos, box = pyoracle.dambreak(SIDE)
+    args = pyoracle.config_args()
     p, v = pos, None
     for _ in range(a.warmup):
-        p, v, _, _ = port.run(p, v, args, sphx.DT, 1, box=box.as_array())
+        p, v, _, _ = port.run(p, v, args, pyoracle.DT, 1, box=box)
     # each step is one full-workload step; the loop stops early once the
     # budget is spent so that a large --steps still ends within minutes
     t0 = time.perf_counter()
     done = 0
-    while done < a.steps and (done == 0 or time.perf_counter() - t0 < a.ref_budget):
-        p, v, _, _ = port.run(p, v, args, sphx.DT, 1, box=box.as_array())
+    while done < max(1, a.steps) and (done == 0 or time.perf_counter() - t0 < a.ref_budget):
+        p, v, _, _ = port.run(p, v, args, pyoracle.DT, 1, box=box)
         done += 1
     t = time.perf_counter() - t0
     val = len(pos) * done / t

@@ -238,8 +238,10 @@ int sphx_update_particles_release(void);
  * right to call cudaMalloc).  Its scratch is one static device array of about
  * 7 MiB per GPU, held until the process exits; n may be at most 131,072
  * (larger n: SPHX_ERR_INVALID).  Calls share that array, so calls whose work
- * overlaps on the GPU race.  The first call on a device looks up the array's
- * address; make it before any stream capture.  Synchronises `stream`. */
+ * overlaps on the GPU race.  It synchronises `stream` and reads a status
+ * word back, so it cannot be called while that stream is being captured into
+ * a CUDA graph.  The array's device address is looked up the first time a
+ * call runs in a CUDA context of a device, and again in any other context. */
 int sphx_density_static(const sphx_settings *s, const void *d_pos4, size_t n, float *d_rho,
                         float *d_prs, void *stream);
 
@@ -315,6 +317,12 @@ int sphx_server_wait(sphx_server *s, uint64_t ticket, double timeout_s);
 int sphx_server_result(sphx_server *s, uint64_t ticket, float *pos3, float *vel3, float *rho,
                        float *prs);
 int sphx_server_stats_get(sphx_server *s, sphx_server_stats *out);
+/* Fault injection on the host, for tests of the failure path (no
+ * counterpart in the reference): the worker's next tick fails with `code`
+ * (negative, an SPHX_ERR_*) as if a CUDA call had.  The server then stops:
+ * every running and queued request ends SPHX_REQ_FAILED with that code, and
+ * waits on them return it at once.  No GPU work is faulted. */
+int sphx_server_inject_failure(sphx_server *s, int code);
 int sphx_server_destroy(sphx_server *s);
 
 #ifdef __cplusplus

@@ -218,6 +218,76 @@ class Port(_Lib):
         return rho, prs, force
 
 
+# ------------------------------------------------------------------ workloads
+#
+# numpy restatements of the product's workload generators, so that the CPU
+# arms (bench.py --impl reference, the oracle side of the parity tests) can
+# build the same inputs without loading the product library.  A test checks
+# each against the product's own generator bit for bit.
+
+GAMMA = np.uint64(0x9E3779B97F4A7C15)
+SPACING = 0.05
+JITTER = 0.0025
+DT = 0.002
+
+
+def mix64(z):
+    """SplitMix64's output function over uint64 arrays."""
+    z = np.asarray(z, np.uint64)
+    with np.errstate(over="ignore"):
+        z = z + GAMMA
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def lattice(nx, ny, nz, origin, spacing, jitter, seed):
+    """The jittered cubic lattice of sphx_lattice: row idx = (k * ny + j) * nx + i,
+    coordinate a = origin[a] + ijk[a] * spacing + (2u - 1) * jitter with u the top
+    24 bits of SplitMix64(seed + (3 idx + a + 1) * gamma) times 2^-24, every
+    operation in float32 in that order."""
+    n = nx * ny * nz
+    idx = np.arange(n, dtype=np.uint64)
+    k, rem = np.divmod(np.arange(n), nx * ny)
+    j, i = np.divmod(rem, nx)
+    ijk = [i, j, k]
+    out = np.zeros((n, 3), np.float32)
+    for a in range(3):
+        with np.errstate(over="ignore"):
+            ctr = np.uint64(seed) + (np.uint64(3) * idx + np.uint64(a)) * GAMMA
+        r = mix64(ctr)
+        u = (r >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24)
+        jit = (u * np.float32(2.0) - np.float32(1.0)) * np.float32(jitter)
+        base = np.float32(origin[a]) + ijk[a].astype(np.float32) * np.float32(spacing)
+        out[:, a] = base + jit
+    return out
+
+
+def config_args(gas_const=20.0, viscosity=1.0):
+    """SPHSettings constructor floats of the benchmark configurations (mass 0.125,
+    rest density 1000, k, mu, h 0.1, g -9.8, tension 0) as float32."""
+    return np.array([0.125, 1000.0, gas_const, viscosity, 0.1, -9.8, 0.0], np.float32)
+
+
+def dambreak(nx, ny=None, nz=None, box_scale=(2.5, 1.25, 1.25), seed=0, h=0.1,
+             spacing=SPACING, jitter=JITTER):
+    """A dam-break block: nx*ny*nz lattice particles in the corner of a box
+    box_scale times the block edges (x, z centred on 0, floor y = 0, no
+    ceiling, damping 0.5, offset 1e-4), starting one spacing inside the
+    reflection planes.  Returns (positions (n, 3) float32, box as the 9-float
+    oracle array)."""
+    ny = nx if ny is None else ny
+    nz = nx if nz is None else nz
+    f = lambda v: float(np.float32(v))  # the box is stored as float32
+    edges = np.array([nx, ny, nz], np.float64) * spacing
+    dims = edges * np.array(box_scale)
+    box = np.array([f(-dims[0] / 2), f(dims[0] / 2), 0.0, f(dims[1]), f(-dims[2] / 2),
+                    f(dims[2] / 2), f(0.5), f(0.0001), 0.0], np.float32)
+    origin = (f(float(box[0]) + h + spacing), f(float(box[2]) + h + spacing),
+              f(float(box[4]) + h + spacing))
+    return lattice(nx, ny, nz, origin, spacing, jitter, seed), box
+
+
 def build():
     """Builds the oracle libraries (restatement always; reference where present)."""
     import importlib.util

@@ -46,35 +46,27 @@ def _compile(src, extra=()):
     if src.endswith(".cu"):
         cmd = [NVCC, *NVCC_FLAGS, *extra, *inc, "-c", src, "-o", obj]
     else:
-        defs = [e for e in extra if e.startswith("-D")]  # variant defines apply to host code too
-        cmd = ["g++", *CXX_FLAGS, *defs, *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c",
-               src, "-o", obj]
+        cmd = ["g++", *CXX_FLAGS, *inc, "-I", os.path.join(CUDA_HOME, "include"), "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("compile failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    if extra and r.stderr:
+        sys.stderr.write(r.stderr)
     return obj, True
 
 
-def build(verbose=False, ptxas_info=False, defines=(), lib=None, build_dir=None):
-    """Compiles every translation unit under csrc/ and links lib/libsphx.so.
-
-    ``defines`` (e.g. ``["SPHX_FORCE_MIN_BLOCKS=2"]``) and ``lib`` /
-    ``build_dir`` build a variant elsewhere, for tuning sweeps."""
-    global BUILD
-    lib = lib or LIB
-    saved = BUILD
-    BUILD = build_dir or BUILD
-    try:
-        return _build(verbose, ptxas_info, ["-D" + d for d in defines], lib)
-    finally:
-        BUILD = saved
-
-
-def _build(verbose, ptxas_info, dflags, LIB):
+def build(verbose=False, ptxas_info=False):
+    """Compiles every translation unit under csrc/ and links lib/libsphx.so
+    (``ptxas_info``: print each kernel's registers, spills and shared memory)."""
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
-    extra = (["-Xptxas", "-v"] if ptxas_info else []) + dflags
+    extra = ["-Xptxas", "-v"] if ptxas_info else []
+    if ptxas_info:  # recompile the CUDA units so that ptxas reports
+        for s in srcs:
+            obj = os.path.join(BUILD, os.path.basename(s) + ".o")
+            if s.endswith(".cu") and os.path.exists(obj):
+                os.remove(obj)
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         results = list(ex.map(lambda s: _compile(s, extra), srcs))
     objs = [o for o, _ in results]

@@ -362,7 +362,7 @@ cudaError_t enqueue_step(sphx_handle *h, bool reorder, int &pv, int &idc, cudaEv
     const sphx::NbrList L{h->nbr, h->ncount, h->opt.neighbor_slots};
     if ((e = sphx::launch_density(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L, !reorder,
                                   st, h->tune.density_threads,
-                                  SPHX_ROW_WARPS ? &h->row_warps : nullptr)) != cudaSuccess)
+                                  &h->row_warps)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[2], st);
     if ((e = sphx::launch_force(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L,
@@ -472,7 +472,7 @@ int sphx::run_steps(sphx_handle *h, float dt, int nsteps) {
             const uint32_t tiles = (h->slots + 1u + 4095u) / 4096u;
             h->launches_per_step[h->events_used / 4] =
                 (reorder ? 12u : 11u) + (tiles > 1024u) +
-                (SPHX_ROW_WARPS ? 1u + (h->rows >= 4096u) : 0u);
+                1u + (h->rows >= 4096u);
             h->events_used += 4;
             int pv = h->pv, idc = h->idc;
             SPHX_CUDA(enqueue_step(h, reorder, pv, idc, ev));

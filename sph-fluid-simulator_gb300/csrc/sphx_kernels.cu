@@ -36,18 +36,12 @@
 #include "sphx_common.h"
 #include "sphx_kernels.h"
 
-// Resident threads per SM the two walk kernels are compiled for (register
-// cap 65536 / threads); the block size is a template parameter chosen per
-// launch (128 or 256, see Tuning).
-#ifndef SPHX_DENSITY_THREADS_PER_SM
-#define SPHX_DENSITY_THREADS_PER_SM 1024
-#endif
-#ifndef SPHX_FORCE_LIST_THREADS_PER_SM
-#define SPHX_FORCE_LIST_THREADS_PER_SM 1024
-#endif
-#ifndef SPHX_FORCE_THREADS_PER_SM
-#define SPHX_FORCE_THREADS_PER_SM 1024
-#endif
+// Resident threads per SM the walk kernels are compiled for (register cap
+// 65536 / threads); the block size is a template parameter chosen per launch
+// (128 or 256, see Tuning).
+constexpr int kDensityThreadsPerSM = 1024;
+constexpr int kForceListThreadsPerSM = 1024;
+constexpr int kForceThreadsPerSM = 1024;
 
 namespace sphx {
 namespace {
@@ -404,15 +398,11 @@ __device__ __forceinline__ void scan_run(const WalkCtx &W, uint32_t a, uint32_t 
 // When some particle lies outside the grid's x extent (xmono false) the run
 // is not monotone in x and candidates past xhi are skipped, not the rest of
 // the run.
-#ifndef SPHX_WINDOW_SEARCH
-#define SPHX_WINDOW_SEARCH 1
-#endif
 
 template <bool kInd, class V>
 __device__ __forceinline__ void scan_run_x(const WalkCtx &W, uint32_t a, uint32_t b, uint32_t self,
                                            float4 pi, float xlo, float xhi, bool xmono, V &vis) {
     uint32_t t = a;
-#if SPHX_WINDOW_SEARCH
     if (xmono) {  // the run is x-sorted: binary search for the first x >= xlo
         uint32_t lo = a, hi = b;
         while (lo < hi) {
@@ -423,7 +413,6 @@ __device__ __forceinline__ void scan_run_x(const WalkCtx &W, uint32_t a, uint32_
         }
         t = lo;
     }
-#endif
     for (; t + 1 < b; t += 2) {
         const uint32_t j0 = kInd ? W.order[t] : t;
         const uint32_t j1 = kInd ? W.order[t + 1] : t + 1;
@@ -644,19 +633,10 @@ __device__ __forceinline__ void walk(const WalkCtx &W, const WalkStart &s, uint3
 // (PosScan: positions, for density and the digest; RecordScan: the force
 // kernel's 32-byte neighbour records).
 // 256 positions (4 KB a warp): fewer chunk rounds per row once cells fill
-// up, 2 % faster than 128 from step 40 of the 2.1M dam-break on
-#ifndef SPHX_COOP_CHUNK
-#define SPHX_COOP_CHUNK 256
-#endif
-#ifndef SPHX_COOP_SEARCH
-#define SPHX_COOP_SEARCH 1
-#endif
-#ifndef SPHX_SCAN_UNROLL
-#define SPHX_SCAN_UNROLL 4
-#endif
-constexpr int kScanUnroll = SPHX_SCAN_UNROLL;
-
-constexpr uint32_t kCoopChunk = SPHX_COOP_CHUNK;
+// up; 2 % faster than 128 positions from step 40 of the 2,097,152-particle
+// dam-break block on, measured with CUDA events on a GB300.
+constexpr int kScanUnroll = 4;
+constexpr uint32_t kCoopChunk = 256;
 
 struct CoopLane {
     bool valid;  // holds a particle that walks
@@ -868,7 +848,6 @@ struct PosScan {
             }
             return false;
         }
-#if SPHX_COOP_SEARCH
         {  // x-sorted: start at the first x >= xlo
             uint32_t l = lo, u = hi;
             while (l < u) {
@@ -878,15 +857,11 @@ struct PosScan {
             }
             lo = l;
         }
-#endif
         // every candidate from the searched start on has x >= xlo
 #pragma unroll kScanUnroll
         for (uint32_t k = lo; k < hi; ++k) {
             const float4 p = sm.p(k);
             if (p.x > xhi) return true;
-#if !SPHX_COOP_SEARCH
-            if (p.x < xlo) continue;
-#endif
             test_pair(W, kInd ? sm.idx[k] : c0 + k, p, self, pi, 1u, vis);
         }
         return false;
@@ -1109,10 +1084,7 @@ constexpr int kDeferredThreads = 128;
 constexpr unsigned kDeferredBlocks = 2 * 152;
 // No list is recorded for a particle whose cell holds more than
 // slots / kListSkipFactor particles; its count then carries kNoList.
-#ifndef SPHX_LIST_SKIP_FACTOR
-#define SPHX_LIST_SKIP_FACTOR 4
-#endif
-constexpr uint32_t kListSkipFactor = SPHX_LIST_SKIP_FACTOR;
+constexpr uint32_t kListSkipFactor = 4;
 constexpr uint32_t kNoList = 0x80000000u;
 
 // A particle's list row, or NULL when its own cell holds so many particles
@@ -1152,7 +1124,7 @@ __device__ __forceinline__ void density_finish(const StepParams &P, const Densit
 // neighbourhood has a bucket collision are listed in `deferred` for
 // k_density_deferred.
 template <bool kInd, int kThreads>
-__global__ void __launch_bounds__(kThreads, SPHX_DENSITY_THREADS_PER_SM / kThreads)
+__global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
               float4 *__restrict__ fr, NbrList L, RowWarps RW, uint32_t *__restrict__ deferred,
               uint32_t *__restrict__ status) {
@@ -1241,14 +1213,9 @@ __device__ __forceinline__ void pair_add_record(ForcePair &pair, float4 a, float
 }
 
 // A neighbour's 32-byte record (32-byte aligned: fr is), read-only during
-// the force pass; one 256-bit load (four 64-bit lanes) where SPHX_REC256 is
-// set.
-#ifndef SPHX_REC256
-#define SPHX_REC256 1
-#endif
+// the force pass: one 256-bit load (four 64-bit lanes).
 __device__ __forceinline__ void load_record(const float4 *__restrict__ fr, uint32_t j, float4 &a,
                                             float4 &b) {
-#if SPHX_REC256
     const float4 *p = fr + 2 * (size_t)j;
     unsigned long long q0, q1, q2, q3;
     asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];" : "=l"(q0), "=l"(q1), "=l"(q2), "=l"(q3) : "l"(p));
@@ -1256,10 +1223,6 @@ __device__ __forceinline__ void load_record(const float4 *__restrict__ fr, uint3
     asm("mov.b64 {%0, %1}, %2;" : "=f"(a.z), "=f"(a.w) : "l"(q1));
     asm("mov.b64 {%0, %1}, %2;" : "=f"(b.x), "=f"(b.y) : "l"(q2));
     asm("mov.b64 {%0, %1}, %2;" : "=f"(b.z), "=f"(b.w) : "l"(q3));
-#else
-    a = fr[2 * (size_t)j];
-    b = fr[2 * (size_t)j + 1];
-#endif
 }
 
 __device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *__restrict__ fr,
@@ -1274,20 +1237,18 @@ __device__ __forceinline__ void pair_from_record(ForcePair &pair, const float4 *
 // mask, then adds the marked pairs; the pair math thus runs with the lanes in
 // step instead of under the acceptance branch (about one candidate in four
 // passes), and every operand comes from shared memory.
-#ifndef SPHX_FORCE_CHUNK
-#define SPHX_FORCE_CHUNK 64
-#endif
+constexpr uint32_t kForceChunk = 64;
 
 template <bool kInd>
 struct RecordSmem {
-    float4 a[SPHX_FORCE_CHUNK];  // x, y, z, pressure
-    float4 b[SPHX_FORCE_CHUNK];  // vx, vy, vz, 1/density
-    uint32_t idx[kInd ? SPHX_FORCE_CHUNK : 1];
+    float4 a[kForceChunk];  // x, y, z, pressure
+    float4 b[kForceChunk];  // vx, vy, vz, 1/density
+    uint32_t idx[kInd ? kForceChunk : 1];
 };
 
 template <bool kInd>
 struct RecordScan {
-    static constexpr uint32_t kChunk = SPHX_FORCE_CHUNK;
+    static constexpr uint32_t kChunk = kForceChunk;
     RecordSmem<kInd> &sm;
     const float4 *__restrict__ fr;
     ForcePair &pair;
@@ -1414,7 +1375,7 @@ __device__ __forceinline__ void force_finish(const StepParams &P, const ForcePai
 // particles) hold one: keeping the walk out of this kernel leaves it 48
 // registers instead of 64 with spills (0.257 against 0.276 ms at 2.1M).
 template <bool kInd, int kThreads>
-__global__ void __launch_bounds__(kThreads, SPHX_FORCE_LIST_THREADS_PER_SM / kThreads)
+__global__ void __launch_bounds__(kThreads, kForceListThreadsPerSM / kThreads)
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
@@ -1467,7 +1428,7 @@ __global__ void __launch_bounds__(kThreads, SPHX_FORCE_LIST_THREADS_PER_SM / kTh
 // Walkers off the cooperative path (bucket collision, grid seam) are listed
 // in `deferred` for k_force_deferred.
 template <bool kInd, int kThreads>
-__global__ void __launch_bounds__(kThreads, SPHX_FORCE_THREADS_PER_SM / kThreads)
+__global__ void __launch_bounds__(kThreads, kForceThreadsPerSM / kThreads)
     k_force_walk(SceneTable T, WalkCtx G, const float4 *__restrict__ vel,
                  const float4 *__restrict__ rp, const float4 *__restrict__ fr, NbrList L,
                  float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
@@ -1811,9 +1772,7 @@ cudaError_t launch_cell_flags(const SceneTable &T, uint32_t slots, uint8_t *cfla
 // on the neighbour records: all of the SM's L1 as cache (carveout 0) took it
 // from 0.268 to 0.261 ms at 2.1M particles.  The density kernel gained
 // nothing either way (it keeps the driver's choice).
-#ifndef SPHX_FORCE_CARVEOUT
-#define SPHX_FORCE_CARVEOUT 0
-#endif
+constexpr int kForceCarveout = 0;
 
 // Preferred shared-memory share of an SM's L1 for a kernel (percent of the
 // maximum; -1 leaves the driver's choice).
@@ -1827,10 +1786,10 @@ static cudaError_t carveout(K *kernel, int percent) {
 cudaError_t prepare_device() {
     cudaError_t e = cudaFuncSetAttribute(k_cellsort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          8 * kLargeCell);
-    if (e == cudaSuccess) e = carveout(k_force<false, 128>, SPHX_FORCE_CARVEOUT);
-    if (e == cudaSuccess) e = carveout(k_force<true, 128>, SPHX_FORCE_CARVEOUT);
-    if (e == cudaSuccess) e = carveout(k_force<false, 256>, SPHX_FORCE_CARVEOUT);
-    if (e == cudaSuccess) e = carveout(k_force<true, 256>, SPHX_FORCE_CARVEOUT);
+    if (e == cudaSuccess) e = carveout(k_force<false, 128>, kForceCarveout);
+    if (e == cudaSuccess) e = carveout(k_force<true, 128>, kForceCarveout);
+    if (e == cudaSuccess) e = carveout(k_force<false, 256>, kForceCarveout);
+    if (e == cudaSuccess) e = carveout(k_force<true, 256>, kForceCarveout);
     return e;
 }
 
@@ -1900,7 +1859,7 @@ static void force_launch(const SceneTable &T, const WalkCtx &G, const float4 *ve
                          cudaStream_t st) {
     // the walkers' kernel: as many warps as the GPU holds at once (or fewer)
     const unsigned walk_blocks =
-        std::min<unsigned>(blocks(T.n, kThreads), 152u * (SPHX_FORCE_THREADS_PER_SM / kThreads));
+        std::min<unsigned>(blocks(T.n, kThreads), 152u * (kForceThreadsPerSM / kThreads));
     if (indirect) {
         k_force<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
             T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);

@@ -78,9 +78,6 @@ constexpr uint32_t kNbrSlotsDefault = 256, kNbrSlotsMax = 1024;
 
 // The density pass's warps, each inside one cell row (see k_row_warps):
 // wofs[R] = first warp of cell row R, rows + 1 entries.
-#ifndef SPHX_ROW_WARPS
-#define SPHX_ROW_WARPS 1
-#endif
 struct RowWarps {
     uint32_t *wofs;
 };

@@ -22,9 +22,13 @@
 //     call's contents: the counts and status words are cleared at the start
 //     of each call, and two calls whose work overlaps on the GPU race on the
 //     array (serialise them, e.g. on one stream);
-//   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current and caches it; make
-//     that first call before any stream capture.
+//   * a call synchronises its stream and reads a status word back, so it
+//     cannot be made while that stream is being captured into a CUDA graph;
+//   * the array's device address is looked up (cudaGetSymbolAddress) with
+//     the device current, the first time a call runs in a given CUDA context
+//     of that device, and cached with that context: a call made in another
+//     context of the same device (after cudaDeviceReset, or a context a
+//     driver-API host made current) looks it up again.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -63,25 +67,57 @@ static_assert(sizeof(sphx::StepParams) + 16 <= 1024, "scene table fits its scrat
 static __device__ __align__(256) uint4 g_scratch[kScratchBytes / sizeof(uint4)];
 
 std::mutex g_mu;
+// Per device: the context the cached address belongs to, and the address.
+void *g_ctx[kMaxDevices] = {};
 char *g_addr[kMaxDevices] = {};
 
-// Device address of g_scratch on the current device (looked up once).
+// The calling thread's current CUDA context (the driver's cuCtxGetCurrent,
+// reached through the runtime so that the library does not link the driver
+// library itself), or NULL when it cannot be determined.
+void *current_context() {
+    using GetCurrent = int (*)(void **);
+    static GetCurrent fn = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<GetCurrent>(f);
+    }();
+    void *ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Device address of g_scratch in the current context of the current device.
+// It is looked up (and the device's kernels prepared) once per context, and
+// cached only once both succeeded.
 int scratch_address(char **out) {
     int dev = 0;
     SPHX_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return sphx::fail(SPHX_ERR_CUDA, "device ordinal out of range");
+    void *ctx = current_context();  // NULL before the runtime made one current
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess)
-            return sphx::fail(SPHX_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_addr[dev] = static_cast<char *>(p);
-        const cudaError_t e2 = sphx::prepare_device();
-        if (e2 != cudaSuccess)
-            return sphx::fail(SPHX_ERR_CUDA, std::string("prepare_device: ") + cudaGetErrorString(e2));
+    if (ctx && g_ctx[dev] == ctx && g_addr[dev]) {
+        *out = g_addr[dev];
+        return SPHX_OK;
     }
-    *out = g_addr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess)
+        return sphx::fail(SPHX_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    const cudaError_t e2 = sphx::prepare_device();
+    if (e2 != cudaSuccess)
+        return sphx::fail(SPHX_ERR_CUDA, std::string("prepare_device: ") + cudaGetErrorString(e2));
+    // the lookup made the device's primary context current if none was;
+    // without a context handle nothing is cached and the next call looks up
+    ctx = current_context();
+    g_ctx[dev] = ctx;
+    g_addr[dev] = ctx ? static_cast<char *>(p) : nullptr;
+    *out = static_cast<char *>(p);
     return SPHX_OK;
 }
 

@@ -65,6 +65,7 @@ struct sphx_server {
     uint64_t next_ticket = 1;
     size_t bytes_in_use = 0;
     bool stop = false;
+    int inject = 0;  // host-side fault injection: the next tick fails with this code
     int fatal = 0;
     std::string fatal_msg;
     sphx_handle *h = nullptr;
@@ -130,6 +131,13 @@ void sphx_server::run() {
         // One tick: every live scene advances by the same number of steps.
         int k = opt.steps_per_tick;
         for (Request *r : live) k = std::min(k, r->nsteps - r->steps_done);
+        {
+            std::lock_guard<std::mutex> g(mu);
+            if (inject) {
+                rc = sphx::fail(inject, "injected failure");
+                inject = 0;
+            }
+        }
         if (rc == SPHX_OK && k > 0) rc = sphx::run_steps(h, opt.dt, k);
         if (rc == SPHX_OK) rc = sphx::read_status(h);
         std::vector<int> finished;
@@ -169,11 +177,20 @@ void sphx_server::run() {
         if (rc != SPHX_OK) {
             fatal = rc;
             fatal_msg = sphx_last_error();
+            // the batch is gone: every request not yet done fails with the
+            // server's error, the queued ones too (nothing will admit them)
             for (Request *r : live) {
                 r->state = SPHX_REQ_FAILED;
                 r->error = rc;
             }
+            for (Request *r : queue) {
+                r->state = SPHX_REQ_FAILED;
+                r->error = rc;
+            }
             live.clear();
+            queue.clear();
+            stats.live_scenes = 0;
+            stats.queued = 0;
             done_cv.notify_all();
             break;
         }
@@ -312,6 +329,14 @@ int sphx_server_result(sphx_server *s, uint64_t ticket, float *pos3, float *vel3
     if (prs) std::copy(r->prs.begin(), r->prs.end(), prs);
     s->all.erase(it);
     delete r;
+    return SPHX_OK;
+}
+
+int sphx_server_inject_failure(sphx_server *s, int code) {
+    using sphx::fail;
+    if (!s || code >= 0) return fail(SPHX_ERR_INVALID, "a server and a negative status code");
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->inject = code;
     return SPHX_OK;
 }
 

@@ -17,8 +17,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# SPHX_LIB names another build of the library (a tuning variant)
-LIB_PATH = os.environ.get("SPHX_LIB") or os.path.join(HERE, "lib", "libsphx.so")
+LIB_PATH = os.path.join(HERE, "lib", "libsphx.so")
 
 SPHX_OK = 0
 ERRORS = {-1: "INVALID", -2: "CUDA", -3: "NOMEM", -4: "DOMAIN", -5: "OVERFLOW", -6: "STATE"}
@@ -167,6 +166,7 @@ def lib():
         "sphx_server_wait": (C.c_int, [vp, C.c_uint64, C.c_double]),
         "sphx_server_result": (C.c_int, [vp, C.c_uint64, vp, vp, vp, vp]),
         "sphx_server_stats_get": (C.c_int, [vp, P(ServerStats)]),
+        "sphx_server_inject_failure": (C.c_int, [vp, C.c_int]),
         "sphx_server_destroy": (C.c_int, [vp]),
         "sphx_set_profiling": (C.c_int, [vp, C.c_int]),
         "sphx_get_kernel_times": (C.c_int, [vp, P(KernelTimes)]),
@@ -562,6 +562,10 @@ class Server:
         _check(lib().sphx_server_result(self.h, ticket, _ptr(out["pos"]), _ptr(out["vel"]),
                                         _ptr(out["rho"]), _ptr(out["prs"])))
         return out
+
+    def inject_failure(self, code=-2):
+        """Makes the worker's next tick fail with `code` (host-side injection)."""
+        _check(lib().sphx_server_inject_failure(self.h, code))
 
     def stats(self):
         st = ServerStats()

@@ -33,35 +33,9 @@ def rel_err(x, y):
     return float((d / np.maximum(ny, floor)).max())
 
 
-GAMMA = np.uint64(0x9E3779B97F4A7C15)
-
-
-def mix64(z):
-    z = np.asarray(z, np.uint64)
-    with np.errstate(over="ignore"):
-        z = z + GAMMA
-        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-    return z ^ (z >> np.uint64(31))
-
-
-def lattice_np(nx, ny, nz, origin, spacing, jitter, seed):
-    """numpy restatement of sphx_lattice (float32 arithmetic, same order)."""
-    n = nx * ny * nz
-    idx = np.arange(n, dtype=np.uint64)
-    k, rem = np.divmod(np.arange(n), nx * ny)
-    j, i = np.divmod(rem, nx)
-    ijk = [i, j, k]
-    out = np.zeros((n, 3), np.float32)
-    for a in range(3):
-        with np.errstate(over="ignore"):
-            ctr = np.uint64(seed) + (np.uint64(3) * idx + np.uint64(a)) * GAMMA
-        r = mix64(ctr)
-        u = (r >> np.uint64(40)).astype(np.float32) * np.float32(2.0 ** -24)
-        jit = (u * np.float32(2.0) - np.float32(1.0)) * np.float32(jitter)
-        base = np.float32(origin[a]) + ijk[a].astype(np.float32) * np.float32(spacing)
-        out[:, a] = base + jit
-    return out
+# The numpy restatements of the workload generators live with the oracle
+# (bench.py's CPU arm uses them too).
+from pyoracle import GAMMA, lattice as lattice_np, mix64  # noqa: E402,F401
 
 
 def header_functions(path=os.path.join(INCLUDE, "sphx.h")):

@@ -65,6 +65,32 @@ def test_batch_vs_oracle(sphx_lib, port):
         first += n
 
 
+def test_512_scene_benchmark_mix_vs_oracle(sphx_lib, port):
+    """The batched benchmark's own 512 scenes (7.7M particles, counts
+    log-uniform in [1000, 65536], per-scene k and mu): one batched step,
+    every scene's fields and neighbour multisets against the oracle's step
+    of that scene alone."""
+    sphx = sphx_lib
+    scenes = sphx.batch_scenes(512, seed=0)
+    with sphx.Scene.batch(scenes) as b:
+        cnt, dig = b.neighbor_digest()
+        b.step(sphx.DT, 1)
+        got = b.read()
+        ranges = [b.scene_range(k) for k in range(len(scenes))]
+    worst = {f: 0.0 for f in ("rho", "prs", "force", "pos", "vel")}
+    for k, (s, pos, box) in enumerate(scenes):
+        first, n = ranges[k]
+        assert n == len(pos)
+        c2, d2 = port.neighbor_digest(pos, s.h)
+        assert np.array_equal(cnt[first:first + n], c2) and np.array_equal(dig[first:first + n], d2), k
+        r = port.step(pos, None, sphx.args_array(s), sphx.DT, box=box.as_array()).by_id()
+        for f in worst:
+            e = rel_err(got[f][first:first + n], getattr(r, f))
+            worst[f] = max(worst[f], e)
+            assert e < REL_TOL, (k, f, e)
+    print("512 scenes, worst error per field:", {f: "%.1e" % e for f, e in worst.items()})
+
+
 def test_tuning_variants_agree(sphx_lib):
     sphx = sphx_lib
     scenes = mixed_scenes(sphx)

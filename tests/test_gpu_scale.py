@@ -1,9 +1,12 @@
-"""Parity at the benchmark's own sizes.  The 262,144-particle scene (64^3
-block in an 8 x 4 x 4 m box) is small enough to compare with the oracle
-directly; at 2,097,152 and 8,000,000 particles the checks are the
-size-independent ones: the neighbour multisets against the oracle's walk
-over the same positions, and results that must not change at all when only
-the storage order or the reorder interval changes."""
+"""Parity at the benchmark's own sizes: the 262,144-particle scene (64^3
+block in an 8 x 4 x 4 m box), the 2,097,152-particle headline block (128^3,
+16 x 8 x 8 m) and the 8,000,000-particle block (200^3, 25 x 12.5 x 12.5 m).
+At each size one step's density, pressure, force, position and velocity are
+compared with the oracle's step (the restatement of updateParticlesCPU,
+src/sph.cpp:195-275) and the accepted-neighbour multisets with the oracle's
+walk over the same positions.  Beside that, the size-independent checks:
+results that must not change at all when only the storage order or the
+reorder interval changes."""
 import numpy as np
 import pytest
 
@@ -32,6 +35,35 @@ def test_262k_one_step_vs_oracle(sphx_lib, port):
     r = port.step(pos, vel, CONFIG_ARGS, 0.002, box=box.as_array()).by_id()
     for f in FIELDS:
         assert rel_err(out[f], getattr(r, f)) < REL_TOL, f
+
+
+def one_step_vs_oracle(sphx, port, side, seed):
+    """One step from the dam-break block with seeded random velocities (so
+    that the viscosity term is exercised), every field against the oracle's
+    step, plus the neighbour multisets of the initial positions."""
+    pos, box = sphx.dambreak(side)
+    vel = np.random.default_rng(seed).normal(0, 0.2, pos.shape).astype(np.float32)
+    with sphx.Scene(settings(sphx), box, pos, vel) as sc:
+        cnt, dig = sc.neighbor_digest()
+        sc.step(0.002, 1)
+        out = sc.read()
+    c2, d2 = port.neighbor_digest(pos, 0.1)
+    assert np.array_equal(cnt, c2) and np.array_equal(dig, d2)
+    del c2, d2
+    r = port.step(pos, vel, CONFIG_ARGS, 0.002, box=box.as_array()).by_id()
+    errs = {f: rel_err(out[f], getattr(r, f)) for f in FIELDS}
+    print("%d particles, one step against the oracle: %s"
+          % (len(pos), {f: "%.1e" % e for f, e in errs.items()}))
+    for f in FIELDS:
+        assert errs[f] < REL_TOL, f
+
+
+def test_2m_one_step_fields_vs_oracle(sphx_lib, port):
+    one_step_vs_oracle(sphx_lib, port, 128, 12)
+
+
+def test_8m_one_step_fields_vs_oracle(sphx_lib, port):
+    one_step_vs_oracle(sphx_lib, port, 200, 13)
 
 
 def test_2m_neighbour_multisets_after_steps(sphx_lib, port):

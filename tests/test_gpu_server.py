@@ -1,9 +1,13 @@
 """Served form: requests admitted while others run, advanced together, each
-result identical to the same scene run alone."""
+result identical to the same scene run alone and in agreement with the
+oracle's run of that scene (src/sph.cpp:195-275 restated); the failure
+path (injected on the host) fails every request, running or queued."""
 import time
 
 import numpy as np
 import pytest
+
+from _util import REL_TOL, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -60,3 +64,55 @@ def test_overlap_in_the_mix(sphx_lib):
     longest = max(range(len(reqs)), key=lambda k: reqs[k][3])
     others_admitted = [sts[k].admit_s for k in range(len(reqs)) if k != longest]
     assert max(others_admitted) < sts[longest].done_s
+
+
+def test_served_results_vs_oracle(sphx_lib, port):
+    """Served results against the oracle: one-step requests within the
+    one-step tolerance on every field; requests of a few steps with positions
+    within it too and velocities, densities and pressures within 1e-3 (chained
+    steps let rounding grow, as in the multi-step parity tests)."""
+    sphx = sphx_lib
+    scenes = sphx.batch_scenes(count=8, seed=21, nmin=500, nmax=8000)
+    steps = [1, 3, 1, 5, 2, 1, 4, 1]
+    with sphx.Server(steps_per_tick=2) as srv:
+        tickets = []
+        for k, ((s, pos, box), n) in enumerate(zip(scenes, steps)):
+            tickets.append(srv.submit(s, box, pos, n))
+            if k == 3:
+                time.sleep(0.01)
+        for t in tickets:
+            srv.wait(t, timeout=120)
+        results = [srv.result(t) for t in tickets]
+    for (s, pos, box), n, res in zip(scenes, steps, results):
+        p, v, rho, prs = port.run(pos, None, sphx.args_array(s), sphx.DT, n, box=box.as_array())
+        assert rel_err(res["pos"], p) < REL_TOL
+        tol = REL_TOL if n == 1 else 1e-3
+        assert rel_err(res["vel"], v) < tol
+        assert rel_err(res["rho"], rho) < tol
+        assert rel_err(res["prs"], prs) < tol
+
+
+def test_failure_fails_running_and_queued_requests(sphx_lib):
+    """A tick that fails (injected on the host, no GPU fault) stops the
+    server: the running request and the one still queued behind the budget
+    both end FAILED with the injected code, and waiting on the queued one
+    returns that error at once instead of running out its timeout."""
+    sphx = sphx_lib
+    (s, pos, box), (s2, pos2, box2) = sphx.batch_scenes(count=2, seed=5, nmin=2000, nmax=3000)
+    with sphx.Server(budget_bytes=1, steps_per_tick=1) as srv:
+        running = srv.submit(s, box, pos, 100000)
+        queued = srv.submit(s2, box2, pos2, 10)
+        t0 = time.time()
+        while srv.status(running).state != sphx.Server.REQ_RUNNING and time.time() - t0 < 60:
+            time.sleep(0.005)
+        assert srv.status(queued).state == sphx.Server.REQ_QUEUED
+        srv.inject_failure(-2)
+        t0 = time.time()
+        for t in (running, queued):
+            with pytest.raises(sphx.SphxError) as e:
+                srv.wait(t, timeout=60)
+            assert e.value.code == -2
+            assert srv.status(t).state == sphx.Server.REQ_FAILED
+        assert time.time() - t0 < 30
+        with pytest.raises(sphx.SphxError):
+            srv.submit(s2, box2, pos2, 1)  # a stopped server takes no requests

@@ -64,6 +64,21 @@ def test_lattice_matches_numpy_restatement(sphx_lib):
         assert np.abs(dev).max() <= 0.0025 + 1e-6 and dev.std() > 0.001
 
 
+def test_oracle_workloads_match_product(sphx_lib):
+    """The oracle side's dam-break blocks and settings (what the CPU arm of
+    bench.py builds without the product library) are the product's, bit for
+    bit: the headline block's corner, a batched-workload block, a served one."""
+    import pyoracle
+    for dims, seed in [((12, 12, 12), 0), ((9, 20, 6), 100003 * 0 + 17), ((31, 7, 13), 7919 + 3)]:
+        a, box_a = sphx_lib.dambreak(*dims, seed=seed)
+        b, box_b = pyoracle.dambreak(*dims, seed=seed)
+        assert np.array_equal(bits(a), bits(b))
+        assert np.array_equal(bits(box_a.as_array()), bits(box_b))
+    for k, mu in [(20.0, 1.0), (13.25, 2.5)]:
+        assert np.array_equal(sphx_lib.args_array(sphx_lib.config_settings(k, mu)),
+                              pyoracle.config_args(k, mu))
+
+
 def test_reference_scene_matches_oracle(sphx_lib, port):
     for w, h in [(8, 0.15), (15, 0.15), (5, 0.1)]:
         assert np.array_equal(bits(sphx_lib.reference_scene(w, h)), bits(port.reference_scene(w, h)))

@@ -1,16 +1,16 @@
-"""The reference-side binding of INTEGRATION.md §1 links against the
-unmodified reference sources and libsphx.so, and the reference's own
+"""The reference-side binding (include/integration/sphGPU_sphx.cpp, a
+replacement for the reference's sphGPU.cu) links against the unmodified
+reference sources and libsphx.so, and the reference's own
 updateParticles(..., onGPU=true) dispatch reaches sphx.
 
 Needs the reference checkout (skipped elsewhere).  Without a GPU the call
 must fail loudly inside sphx (no CPU fallback); with one it must succeed."""
 import os
-import re
 import subprocess
 
 import pytest
 
-from _util import INCLUDE, ORACLE, PKG, ROOT
+from _util import INCLUDE, ORACLE, PKG
 
 MAIN = r"""
 #include <cstdio>
@@ -49,10 +49,7 @@ int main() {
 """
 
 
-def stub_source():
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    blocks = re.findall(r"```cpp\n(.*?)```", text, flags=re.S)
-    return next(b for b in blocks if "sphGPU_sphx.cpp" in b)
+STUB = os.path.join(INCLUDE, "integration", "sphGPU_sphx.cpp")
 
 
 def test_reference_links_against_sphx_and_dispatches(sphx_lib, tmp_path):
@@ -60,12 +57,11 @@ def test_reference_links_against_sphx_and_dispatches(sphx_lib, tmp_path):
     src = os.path.join(build_oracle.reference_dir(), "src")
     if not os.path.isfile(os.path.join(src, "sph.cpp")):
         pytest.skip("reference checkout not present")
-    (tmp_path / "stub.cpp").write_text(stub_source())
     (tmp_path / "main.cpp").write_text(MAIN)
     libdir = os.path.join(PKG, "lib")
     exe = str(tmp_path / "ref_with_sphx")
     cmd = ["g++", "-O1", "-std=c++17", "-w", "-pthread", "-I", os.path.join(ORACLE, "shim"), "-I", src,
-           "-I", INCLUDE, str(tmp_path / "stub.cpp"), str(tmp_path / "main.cpp"),
+           "-I", INCLUDE, STUB, str(tmp_path / "main.cpp"),
            os.path.join(src, "sph.cpp"), os.path.join(src, "neighborTable.cpp"),
            os.path.join(src, "timer.cpp"), "-L", libdir, "-lsphx", "-Wl,-rpath," + libdir, "-o", exe]
     subprocess.run(cmd, check=True, capture_output=True, text=True)

@@ -57,6 +57,39 @@ def test_static_scratch_entry_point_matches_resident_path(sphx_lib):
         assert rel_err(prs_s, prs_r) < REL_TOL
 
 
+def test_static_scratch_aliased_grid_matches_resident_path(sphx_lib):
+    """A block 7 m long in x at h = 0.1 covers cells -35..34, wider than the
+    entry point's fixed 64-cell grid: cells then share grid slots and the walk
+    takes its slower, non-monotone path.  Results must not change."""
+    sphx = sphx_lib
+    s = sphx.config_settings()
+    pos, box = sphx.dambreak(140, 6, 6, box_dims=(7.6, 2.0, 2.0), seed=3)
+    assert pos[:, 0].max() - pos[:, 0].min() > 6.4
+    rho_s, prs_s = static_density(sphx, s, pos)
+    rho_r, prs_r = resident_density(sphx, s, pos, box)
+    assert rel_err(rho_s, rho_r) < REL_TOL
+    assert rel_err(prs_s, prs_r) < REL_TOL
+
+
+def test_static_scratch_rejects_non_finite_position(sphx_lib):
+    import torch
+    sphx = sphx_lib
+    L = sphx.lib()
+    s = sphx.config_settings()
+    pos, _ = sphx.dambreak(10, seed=4)
+    p4 = torch.zeros((len(pos), 4), dtype=torch.float32, device="cuda")
+    p4[:, :3] = torch.from_numpy(pos).cuda()
+    p4[17, 1] = float("nan")
+    out = torch.zeros(len(pos), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    rc = L.sphx_density_static(C.byref(s), p4.data_ptr(), len(pos), out.data_ptr(), out.data_ptr(),
+                               None)
+    assert rc == -4  # SPHX_ERR_DOMAIN
+    # the array is usable again by the next call
+    rho_s, _ = static_density(sphx, s, pos)
+    assert np.isfinite(rho_s).all()
+
+
 def test_static_scratch_rejects_oversize(sphx_lib):
     import torch
     sphx = sphx_lib
