@@ -247,31 +247,26 @@ def serve_requests(count, seed=1):
     return reqs
 
 
-def run_serve(a):
+def serve_sweep(sphx, count, rates, tick, device):
     """Poisson arrivals at each rate: p50/p95/p99 completion latency and
     scenes/s of the continuous-batching server, against the same stream
     served one request at a time through the plain path (FIFO: each request
     starts when both it has arrived and the previous one has finished, with
-    its measured service time)."""
-    import torch
-    import sphx
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    reqs = serve_requests(a.requests, seed=1)
-    # service time of each request alone (plain path, end to end)
+    its measured service time, each request measured alone once)."""
+    reqs = serve_requests(count, seed=1)
     service = []
     for s, pos, box, nsteps in reqs:
         t0 = time.perf_counter()
-        with sphx.Scene(s, box, pos, None, sphx.default_options(device=local)) as one:
+        with sphx.Scene(s, box, pos, None, sphx.default_options(device=device)) as one:
             one.step(sphx.DT, nsteps)
             one.read()
         service.append(time.perf_counter() - t0)
     results = []
     rng = np.random.default_rng(2)
-    for lam in [float(x) for x in a.rates.split(",")]:
+    q = lambda x, p: float(np.percentile(x, p))
+    for lam in rates:
         arrivals = np.cumsum(rng.exponential(1.0 / lam, len(reqs)))
         arrivals -= arrivals[0]
-        # sequential plain FIFO
         end = 0.0
         lat_seq = []
         for t_arr, svc in zip(arrivals, service):
@@ -279,8 +274,7 @@ def run_serve(a):
             end = start + svc
             lat_seq.append(end - t_arr)
         span_seq = end - arrivals[0]
-        # continuous batching
-        with sphx.Server(budget_bytes=150e9, steps_per_tick=a.tick, device=local) as srv:
+        with sphx.Server(budget_bytes=150e9, steps_per_tick=tick, device=device) as srv:
             t0 = time.perf_counter()
             tickets = []
             for (s, pos, box, nsteps), t_arr in zip(reqs, arrivals):
@@ -289,25 +283,38 @@ def run_serve(a):
                     time.sleep(delay)
                 tickets.append(srv.submit(s, box, pos, nsteps))
             for t in tickets:
-                srv.wait(t, timeout=600)
+                srv.wait(t, timeout=1200)
             sts = [srv.status(t) for t in tickets]
             for t in tickets:
                 srv.result(t)
-        lat = np.array([st.done_s - st.submit_s for st in sts])
-        span = max(st.done_s for st in sts) - min(st.submit_s for st in sts)
-        q = lambda x, p: float(np.percentile(x, p))
-        results.append({"rate_per_s": lam, "requests": len(reqs),
+            st = srv.stats()
+        lat = np.array([x.done_s - x.submit_s for x in sts])
+        span = max(x.done_s for x in sts) - min(x.submit_s for x in sts)
+        results.append({"rate_per_s": lam,
                         "served": {"scenes_per_s": len(reqs) / span, "p50_s": q(lat, 50),
-                                   "p95_s": q(lat, 95), "p99_s": q(lat, 99)},
+                                   "p95_s": q(lat, 95), "p99_s": q(lat, 99),
+                                   "relayouts": int(st.relayouts), "ticks": int(st.ticks)},
                         "sequential": {"scenes_per_s": len(reqs) / span_seq, "p50_s": q(lat_seq, 50),
-                                       "p95_s": q(lat_seq, 95), "p99_s": q(lat_seq, 99)}})
+                                       "p95_s": q(lat_seq, 95), "p99_s": q(lat_seq, 99)},
+                        "speedup": span_seq / span})
+    n_ps = sum(len(p) * k for _, p, _, k in reqs)
+    return {"requests": len(reqs), "particle_steps": n_ps, "steps_per_tick": tick,
+            "hbm_budget_gb": 150, "rates": results,
+            "workload": "requests: N log-uniform [2000, 500000], steps U[100, 2000], k U[10,40], "
+                        "mu U[0.5,3], dam-break blocks; sequential arm: each request alone through "
+                        "the plain path (create, steps, readout), FIFO over the same arrivals"}
+
+
+def run_serve(a):
+    import torch
+    import sphx
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    res = serve_sweep(sphx, a.requests, [float(x) for x in a.rates.split(",")], a.tick, local)
     line = {"metric": "served scenes/s and completion latency", "unit": "scenes/s",
-            "value": results[-1]["served"]["scenes_per_s"], "higher_is_better": True, "n_gpus": 1,
-            "dtype": "f32", "data": "synthetic (seeded Poisson stream)",
-            "config": {"workload": "requests: N log-uniform [2000, 500000], steps U[100, 2000], "
-                                   "k U[10,40], mu U[0.5,3]; HBM budget 150 GB",
-                       "steps_per_tick": a.tick},
-            "rates": results}
+            "value": res["rates"][-1]["served"]["scenes_per_s"], "higher_is_better": True,
+            "n_gpus": 1, "dtype": "f32", "data": "synthetic (seeded Poisson stream)",
+            "config": {"workload": res["workload"], "steps_per_tick": a.tick}, "served": res}
     print(json.dumps(line), flush=True)
 
 
@@ -363,6 +370,47 @@ def run_reference(a):
                                        % (done, a.warmup)},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+SIDE_8M = 200  # 200^3 = 8,000,000 particles
+REORDER_SWEEP = (1, 4, 16, 64)
+
+
+def configured_run(sphx, torch, s, box, pos, device, steps, reorder, phases, peak):
+    """`steps` steps from the initial lattice as CUDA-graph replays, timed with
+    CUDA events on the scene's stream.  With `phases`, the same run again as
+    plain launches with per-phase events (sort, density, force) for the
+    roofline of the whole run."""
+    n = len(pos)
+    out = {"steps": steps, "reorder_interval": reorder}
+    with sphx.Scene(s, box, pos, None, sphx.default_options(device=device, use_graph=1,
+                                                           reorder_interval=reorder)) as sc:
+        stream = torch.cuda.ExternalStream(sc.device_view().stream, device=device)
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        sc.step(sphx.DT, steps)
+        c1.record(stream)
+        sc.synchronize()
+        ms = max_over_ranks(c0.elapsed_time(c1))
+    out["ms_per_step"] = ms / steps
+    out["particle_steps_per_s"] = n * steps / (ms / 1e3)
+    if phases:
+        with sphx.Scene(s, box, pos, None, sphx.default_options(device=device, use_graph=0,
+                                                               reorder_interval=reorder)) as sc:
+            sc.set_profiling(True)
+            sc.kernel_times()
+            sc.step(sphx.DT, steps)
+            kt = sc.kernel_times()
+        d, f = kt.density_ms / max(kt.steps, 1), kt.force_ms / max(kt.steps, 1)
+        achieved = ALGO_BYTES * n / ((d + f) / 1e3) / 1e9
+        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                           "frac": achieved / peak, "kernels": "k_density + k_force",
+                           "per_step_ms": {"sort": kt.sort_ms / max(kt.steps, 1), "density": d,
+                                           "force": f},
+                           "note": "mean over the whole run, plain launches with per-phase events"}
+    out["note"] = "whole configured run from the initial lattice, CUDA graph replay"
+    return out
 
 
 def run_sphx(a):
@@ -461,32 +509,49 @@ def run_sphx(a):
            "path": "sphx_set_state + sphx_step + sphx_read_state (pinned host buffers)"}
     sc.close()
 
-    # The configured run (200 steps from the initial lattice, graph replay):
-    # the fluid clumps as it falls (the reference's physics at these
-    # constants), so later steps cost more than the timed window above.
-    config_run = None
+    # The configured runs (200 steps from the initial lattice): the fluid
+    # clumps as it falls (the reference's physics at these constants), so
+    # later steps cost more than the timed window above.  The headline block
+    # and the 8M block, each at reorder intervals 1, 4, 16 and 64.
+    peak_hbm = peaks()[0]
+    config_run, sweep_8m, reorder_sweep = None, None, []
     if a.config_steps > 0:
-        sc = sphx.Scene(s, box, pos, None, sphx.default_options(device=device, use_graph=1))
-        stream = torch.cuda.ExternalStream(sc.device_view().stream, device=device)
-        c0 = torch.cuda.Event(enable_timing=True)
-        c1 = torch.cuda.Event(enable_timing=True)
-        c0.record(stream)
-        sc.step(sphx.DT, a.config_steps)
-        c1.record(stream)
-        sc.synchronize()
-        cms = max_over_ranks(c0.elapsed_time(c1))
-        sc.close()
-        config_run = {"steps": a.config_steps, "ms_per_step": cms / a.config_steps,
-                      "particle_steps_per_s": n * a.config_steps * world / (cms / 1e3),
-                      "note": "whole configured run from the initial lattice, CUDA graph replay"}
+        t_sec = time.perf_counter()
+        for side in (SIDE, SIDE_8M):
+            if side == SIDE:
+                p_s, b_s = pos, box
+            else:
+                p_s, b_s = sphx.dambreak(side)
+            for R in REORDER_SWEEP:
+                r = configured_run(sphx, torch, s, b_s, p_s, device, a.config_steps, R,
+                                   phases=(R == 1), peak=peak_hbm)
+                r["particles"] = len(p_s)
+                reorder_sweep.append({k: r[k] for k in ("particles", "reorder_interval", "ms_per_step",
+                                                       "particle_steps_per_s")})
+                if R == 1 and side == SIDE:
+                    config_run = r
+                if R == 1 and side == SIDE_8M:
+                    sweep_8m = r
+            del p_s, b_s
+        sweep_s = time.perf_counter() - t_sec
 
     if rank != 0:
         return
+    section_s = {"sweeps": round(sweep_s, 1) if a.config_steps > 0 else 0.0}
+    t_sec = time.perf_counter()
     cpu = cpu_baseline(pos, box, s) if world == 1 and not a.no_cpu else None
+    section_s["cpu_baseline"] = round(time.perf_counter() - t_sec, 1)
     batched = None
     if world == 1 and a.batch_steps > 0:
-        import sphx
+        t_sec = time.perf_counter()
         batched = batch_compare(sphx.batch_scenes(512, seed=0), a.batch_steps, 0, device)
+        section_s["batched"] = round(time.perf_counter() - t_sec, 1)
+    served = None
+    if world == 1 and a.requests > 0 and a.served_rates:
+        t_sec = time.perf_counter()
+        served = serve_sweep(sphx, a.requests, [float(x) for x in a.served_rates.split(",")],
+                             a.tick, device)
+        section_s["served"] = round(time.perf_counter() - t_sec, 1)
     # state, ids, density, sort scratch, neighbour records and the list entries in use
     ws_mb = (n * (16 * 4 + 4 * 2 + 16 + 12 + 8 + 32) + 4 * pairs) / 1e6
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
@@ -499,7 +564,8 @@ def run_sphx(a):
                        "parallelism": "replicas" if world > 1 else "single"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "clocks": clk.summary(), "gpu_launches": int(kt.launches), "batched": batched,
-            "config_run": config_run}
+            "config_run": config_run, "sweep_8m": sweep_8m, "reorder_sweep": reorder_sweep,
+            "served": served, "section_s": section_s}
     print(json.dumps(line), flush=True)
 
 
@@ -511,9 +577,12 @@ def main():
     ap.add_argument("--impl", default="sphx", choices=["sphx", "reference"])
     ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "steps"])
     ap.add_argument("--side", type=int, default=SIDE, help="block side of --workload steps")
-    ap.add_argument("--batch-steps", type=int, default=20,
+    ap.add_argument("--batch-steps", type=int, default=200,
                     help="steps of the batched-vs-sequential comparison in the plain run (0: skip)")
-    ap.add_argument("--requests", type=int, default=32)
+    ap.add_argument("--requests", type=int, default=64,
+                    help="requests of the served comparison (0: skip it in the plain run)")
+    ap.add_argument("--served-rates", default="50,200,1000,2000",
+                    help="arrival rates of the served comparison in the plain run ('': skip)")
     ap.add_argument("--config-steps", type=int, default=200,
                     help="steps of the whole-configuration run reported as config_run (0: skip)")
     ap.add_argument("--rates", default="50,100,200,500,1000,2000")

@@ -361,8 +361,7 @@ cudaError_t enqueue_step(sphx_handle *h, bool reorder, int &pv, int &idc, cudaEv
     if (ev) cudaEventRecord(ev[1], st);
     const sphx::NbrList L{h->nbr, h->ncount, h->opt.neighbor_slots};
     if ((e = sphx::launch_density(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L, !reorder,
-                                  st, h->tune.density_threads,
-                                  &h->row_warps)) != cudaSuccess)
+                                  st, h->tune.density_threads, h->row_warps)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[2], st);
     if ((e = sphx::launch_force(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L,

@@ -951,34 +951,10 @@ __device__ __forceinline__ uint32_t row_of_warp(const uint32_t *__restrict__ wof
     return lo;
 }
 
-// Thread g's particle: its cell-sorted position t, whether it has one
-// (valid) and, with row warps, its scene.  False when the whole warp has
-// nothing to do (the cooperative walk needs every lane, so warps leave
-// together).
-__device__ __forceinline__ bool thread_particle(const SceneTable &T, const uint32_t *__restrict__ start,
-                                                const RowWarps &RW, uint32_t g, uint32_t &t,
-                                                bool &valid, uint32_t &sc) {
-    sc = 0;
-    if (RW.wofs) {  // one cell row per warp
-        const uint32_t w = g >> 5;
-        if (w >= RW.wofs[T.rows]) return false;
-        const uint32_t R = row_of_warp(RW.wofs, T.rows, w);
-        sc = scene_of_row(T, R);
-        const uint32_t f = row_first_slot(T, sc, R);
-        t = start[f] + ((w - RW.wofs[R]) << 5) + (threadIdx.x & 31u);
-        valid = t < start[f + (uint32_t)T.params[sc].grid.gx];
-        return true;
-    }
-    if ((g & ~31u) >= T.n) return false;
-    t = g;
-    valid = t < T.n;
-    return true;
-}
-
-// Threads a launch needs: with row warps at most n / 32 + rows warps (a
-// row's last warp is partial).
-__host__ __forceinline__ uint32_t launch_threads(const SceneTable &T, const RowWarps &RW) {
-    return RW.wofs ? (T.n / 32u + T.rows + 1u) * 32u : T.n;
+// Threads a density launch needs: at most n / 32 + rows warps (each row's
+// last warp is partial).
+__host__ __forceinline__ uint32_t launch_threads(const SceneTable &T) {
+    return (T.n / 32u + T.rows + 1u) * 32u;
 }
 
 // Kernel 1, kScanTile rows per block: every row's warp count, scanned within
@@ -1042,6 +1018,18 @@ __device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
     s = t;
 }
 
+// kahan_add of u^3, the cube's last product fused into the compensation
+// step: u^3 - c is rounded once instead of twice.  As accurate as the plain
+// form (checked on the CPU against an FP64 sum over the dam-break block) and
+// one instruction shorter.
+__device__ __forceinline__ void kahan_add_cube(float &s, float &c, float u) {
+    const float u2 = __fmul_rn(u, u);
+    const float y = __fmaf_rn(u2, u, -c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
 // Accepted neighbours of a particle, in walk order, are also recorded for
 // the force kernel: entry k of particle i is nbr[i * slots + k], k < slots
 // (one contiguous row per particle, written by one lane front to back); a
@@ -1055,8 +1043,7 @@ struct DensityVisitor {
     uint32_t slots;
     uint32_t cnt;
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float d2) {
-        const float u = __fsub_rn(h2, d2);
-        kahan_add(acc, comp, __fmul_rn(__fmul_rn(u, u), u));
+        kahan_add_cube(acc, comp, __fsub_rn(h2, d2));
         // streaming store: the force pass reads the row once, after every
         // other row has been written
         if (row && cnt < slots) __stcs(row + cnt, j);
@@ -1100,16 +1087,19 @@ __device__ __forceinline__ uint32_t *density_row(const WalkCtx &W, const WalkSta
     return occ * kListSkipFactor <= L.slots ? L.nbr + (size_t)i * L.slots : nullptr;
 }
 
-// Density, pressure, the list count and the neighbour record of particle i.
-__device__ __forceinline__ void density_finish(const StepParams &P, const DensityVisitor &v,
-                                               uint32_t i, float4 pi, const float4 *__restrict__ vel,
+// Density, pressure, the list count and the neighbour record of particle i
+// from its compensated sum of cubes `acc` and its accepted count (`listed`:
+// whether a list row was recorded).
+__device__ __forceinline__ void density_finish(const StepParams &P, float acc, uint32_t cnt,
+                                               bool listed, uint32_t i, float4 pi,
+                                               const float4 *__restrict__ vel,
                                                float4 *__restrict__ rp, float4 *__restrict__ fr,
                                                const NbrList &L) {
-    const float rho = __fadd_rn(__fmul_rn(P.mp6, v.acc), P.selfDens);
+    const float rho = __fadd_rn(__fmul_rn(P.mp6, acc), P.selfDens);
     const float prs = __fmul_rn(P.gasConstant, __fsub_rn(rho, P.restDensity));
     const float inv = __frcp_rn(rho);
     rp[i] = make_float4(rho, prs, inv, 0.f);
-    if (L.nbr) L.count[i] = v.row ? v.cnt : (v.cnt | kNoList);
+    if (L.nbr) L.count[i] = listed ? cnt : (cnt | kNoList);
     if (fr) {
         // what the force kernel reads of a neighbour, in one 32-byte record
         const float4 vi = vel[i];
@@ -1118,34 +1108,150 @@ __device__ __forceinline__ void density_finish(const StepParams &P, const Densit
     }
 }
 
-// Density and pressure, sph.cpp:28-76.  The reference accumulates
-// m*poly6*(h^2-r^2)^3 term by term; here the cubes are summed (compensated)
-// and scaled once: the two differ by float rounding only.  Particles whose
-// neighbourhood has a bucket collision are listed in `deferred` for
+// One lane's scan of chunk slots [lo, hi) of a neighbour row (the chunk
+// holds cell-sorted positions c0, c0 + 1, ...): every candidate inside the
+// lane's x window is tested with the reference's float r^2 (sph.cpp:57: (dx*dx
+// + dy*dy) + dz*dz, no fused multiply-add); an accepted one adds
+// (h^2 - r^2)^3 to the compensated sum and its index to the list row (while
+// it has room).  x-sorted runs (xmono): start at the first x >= xlo
+// (binary search), stop at the first x > xhi; returns true once past the
+// window.  Otherwise every slot is checked against the window.
+template <bool kInd>
+__device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c0, uint32_t lo,
+                                             uint32_t hi, float xlo, float xhi, bool xmono,
+                                             float4 pi, float h2, uint32_t self, float &ks,
+                                             float &kc, uint32_t &cnt, uint32_t *lrow,
+                                             uint32_t lcap) {
+    auto visit = [&](uint32_t k, float4 p) {
+        const float dx = __fsub_rn(p.x, pi.x);
+        const float dy = __fsub_rn(p.y, pi.y);
+        const float dz = __fsub_rn(p.z, pi.z);
+        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        if (d2 < h2 && c0 + k != self) {
+            kahan_add_cube(ks, kc, __fsub_rn(h2, d2));
+            // streaming store: the force pass reads the row once, after
+            // every other row has been written
+            if (cnt < lcap) __stcs(lrow + cnt, kInd ? sm.idx[k] : c0 + k);
+            ++cnt;
+        }
+    };
+    if (!xmono) {
+        for (uint32_t k = lo; k < hi; ++k) {
+            const float4 p = sm.pos[k];
+            if (p.x >= xlo && p.x <= xhi) visit(k, p);
+        }
+        return false;
+    }
+    uint32_t l = lo, u = hi;
+    while (l < u) {
+        const uint32_t mid = (l + u) >> 1;
+        if (sm.pos[mid].x < xlo) l = mid + 1;
+        else u = mid;
+    }
+#pragma unroll kScanUnroll
+    for (uint32_t k = l; k < hi; ++k) {
+        const float4 p = sm.pos[k];
+        if (p.x > xhi) return true;
+        visit(k, p);
+    }
+    return false;
+}
+
+// Density and pressure, sph.cpp:28-76, one warp per cell-row segment (the
+// warps k_row_warps counted).  The reference accumulates m*poly6*(h^2-r^2)^3
+// term by term; here the cubes are summed (compensated) and scaled once: the
+// two differ by float rounding only.
+//
+// A warp's particles are up to 32 consecutive cell-sorted particles of one
+// row of slots (my, mz), hence x-sorted, and share its nine neighbour rows.
+// Row, scene and grid are warp-uniform.  For each neighbour row (dz, then dy,
+// the order walk_rows visits them) the warp copies the union of its lanes'
+// three-cell runs into its shared-memory chunk (coalesced, kCoopChunk
+// positions at a time) and every lane scans its own x window of its own run
+// there (density_scan); a row the narrowing rules out for every lane is
+// skipped.  The pairs and their order are walk_rows': the neighbour lists,
+// recorded in that order, are what the force pass and its walkers sum over.
+// Lanes off this path (a bucket collision, or a slot at the grid's x seam,
+// whose three x-adjacent cells are not one run) are listed for
 // k_density_deferred.
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
               float4 *__restrict__ fr, NbrList L, RowWarps RW, uint32_t *__restrict__ deferred,
               uint32_t *__restrict__ status) {
+    __shared__ PosSmem<kInd> s_chunk[kThreads / 32];
     if (status[0] & kStatusErrorMask) return;
-    uint32_t t, sc;
-    bool valid;
-    if (!thread_particle(T, G.start, RW, blockIdx.x * blockDim.x + threadIdx.x, t, valid, sc)) return;
-    const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
-    if (!RW.wofs) sc = valid ? scene_of(T, i) : 0u;
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= RW.wofs[T.rows]) return;  // whole warps leave together
+    // the warp's row of slots and its scene (warp-uniform)
+    const uint32_t R = row_of_warp(RW.wofs, T.rows, w);
+    const uint32_t sc = scene_of_row(T, R);
     const StepParams &P = T.params[sc];
     const WalkCtx W = walk_ctx(T, G, sc, P, status);
-    const float4 pi = W.pos[i];
+    const Grid &g = W.grid;
+    const uint32_t gx = (uint32_t)g.gx, gy = (uint32_t)g.gy;
+    const uint32_t Rl = R - T.rofs[sc];  // my + gy * mz
+    const int my = (int)(Rl % gy), mz = (int)(Rl / gy);
+    const uint32_t f = Rl * gx;
+    const uint32_t t = W.start[f] + ((w - RW.wofs[R]) << 5) + lane;
+    const bool valid = t < W.start[f + gx];
+    const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
+    const float4 pi = G.pos[i];
     WalkStart s;
     walk_start(W, P, pi, s);
-    const bool slow = valid && s.flags != 0u;
-    defer_lanes(slow, t, deferred, &status[kStatusDeferred]);
-    DensityVisitor v{P.h2, 0.f, 0.f, valid && !slow ? density_row(W, s, L, i) : nullptr, L.slots, 0u};
-    __shared__ PosSmem<kInd> s_coop[kThreads / 32];
-    PosScan<kInd, DensityVisitor> scan{s_coop[threadIdx.x >> 5], v};
-    coop_walk<kInd, false, kTailRows>(W, s, coop_lane(valid, sc, W, s), i, pi, scan, v);
-    if (valid && !slow) density_finish(P, v, i, pi, vel, rp, fr, L);
+    const bool fast = valid && s.flags == 0u && s.mx >= 1 && s.mx + 1 < g.gx;
+    defer_lanes(valid && !fast, t, deferred, &status[kStatusDeferred]);
+    if (!__any_sync(0xffffffffu, fast)) return;
+    const uint32_t mxlo = __reduce_min_sync(0xffffffffu, fast ? (uint32_t)s.mx : 0xffffffffu);
+    const uint32_t mxhi = __reduce_max_sync(0xffffffffu, fast ? (uint32_t)s.mx : 0u);
+    // narrowing: lower bounds on the distance to the rows above and below
+    const float h = P.h;
+    const float eym = gap_to_cell(pi.y, s.c.cy, -1, h), eyp = gap_to_cell(pi.y, s.c.cy, 1, h);
+    const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
+    const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
+    uint32_t *lrow = fast ? density_row(W, s, L, i) : nullptr;
+    const uint32_t lcap = lrow ? L.slots : 0u;
+    float ks = 0.f, kc = 0.f;
+    uint32_t cnt = 0u;
+    PosSmem<kInd> &sm = s_chunk[threadIdx.x >> 5];
+#pragma unroll 1
+    for (int dz = -1; dz <= 1; ++dz) {
+        const float ez2 = dz < 0 ? ezm * ezm : (dz > 0 ? ezp * ezp : 0.f);
+        const uint32_t zrow = (uint32_t)wrap1(mz + dz, g.gz) * gy;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const float ey2 = dy < 0 ? eym * eym : (dy > 0 ? eyp * eyp : 0.f);
+            const float w2 = W.h2w - ey2 - ez2;
+            const bool need = fast && w2 > 0.f;
+            if (!__any_sync(0xffffffffu, need)) continue;
+            const uint32_t base = (zrow + (uint32_t)wrap1(my + dy, g.gy)) * gx;
+            const uint32_t A = W.start[base + mxlo - 1], B = W.start[base + mxhi + 2];
+            uint32_t a = 0u, b = 0u;
+            if (need) {
+                a = W.start[base + s.mx - 1];
+                b = W.start[base + s.mx + 2];
+            }
+            const float hx = need ? fmaf(sqrtf(w2), 1.0000009536743164f, xpad) : 0.f;
+            const float xlo = pi.x - hx, xhi = pi.x + hx;
+            bool done = !need || a == b;
+#pragma unroll 1
+            for (uint32_t c0 = A; c0 < B; c0 += kCoopChunk) {
+                const uint32_t m = min(kCoopChunk, B - c0);
+                for (uint32_t k = lane; k < m; k += 32u) {
+                    const uint32_t j = kInd ? G.order[c0 + k] : c0 + k;
+                    sm.pos[k] = G.pos[j];
+                    if (kInd) sm.idx[k] = j;
+                }
+                __syncwarp();
+                if (!done && b > c0 && a < c0 + m)
+                    done = density_scan<kInd>(sm, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo, xhi,
+                                              W.xmono, pi, W.h2, t, ks, kc, cnt, lrow, lcap);
+                __syncwarp();
+            }
+        }
+    }
+    if (fast) density_finish(P, ks, cnt, lrow != nullptr, i, pi, vel, rp, fr, L);
 }
 
 // The particles k_density deferred, one warp each (warp_walk).
@@ -1171,7 +1277,7 @@ __global__ void __launch_bounds__(kDeferredThreads)
         DensityVisitor v{P.h2, 0.f, 0.f, lane == 0 ? density_row(W, s, L, i) : nullptr, L.slots, 0u};
         PosScan<kInd, DensityVisitor> scan{s_chunk[threadIdx.x >> 5], v};
         warp_walk<kInd>(W, s, i, pi, scan);
-        if (lane == 0) density_finish(P, v, i, pi, vel, rp, fr, L);
+        if (lane == 0) density_finish(P, v.acc, v.cnt, v.row != nullptr, i, pi, vel, rp, fr, L);
     }
 }
 
@@ -1815,8 +1921,7 @@ template <int kThreads>
 static void density_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel, float4 *rp,
                            float4 *fr, const NbrList &L, const RowWarps &RW, bool indirect,
                            uint32_t *deferred, uint32_t *status, cudaStream_t st) {
-    // with row warps: at most n / 32 + rows warps (each row's last is partial)
-    const uint32_t threads = launch_threads(T, RW);
+    const uint32_t threads = launch_threads(T);
     if (indirect) {
         k_density<true, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(
             T, G, vel, rp, fr, L, RW, deferred, status);
@@ -1832,17 +1937,14 @@ static void density_launch(const SceneTable &T, const WalkCtx &G, const float4 *
 
 cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                            const float4 *vel, float4 *rp, float4 *fr, const NbrList &L,
-                           bool indirect, cudaStream_t st, int threads, const RowWarps *rw) {
+                           bool indirect, cudaStream_t st, int threads, const RowWarps &RW) {
+    if (!T.rofs || !T.rows || !RW.wofs) return cudaErrorInvalidValue;
     const WalkCtx G = global_ctx(B, pos);
-    RowWarps RW{nullptr};
-    if (T.n && rw && T.rofs && T.rows) {
+    if (T.n) {
         // rows + 1 scan entries; the sort's tile sums are free again
         const uint32_t ntiles = (T.rows + 1 + kScanTile - 1) / kScanTile;
-        k_row_warps<<<ntiles, kScanThreads, 0, st>>>(T, B.start, rw->wofs, B.tile_sum, B.status);
-        if (ntiles > 1) k_row_offsets<<<ntiles, kScanThreads, 0, st>>>(T.rows, rw->wofs, B.tile_sum);
-        RW = *rw;
-    }
-    if (T.n) {
+        k_row_warps<<<ntiles, kScanThreads, 0, st>>>(T, B.start, RW.wofs, B.tile_sum, B.status);
+        if (ntiles > 1) k_row_offsets<<<ntiles, kScanThreads, 0, st>>>(T.rows, RW.wofs, B.tile_sum);
         // both deferred counts, the walker warps' count and their next one
         cudaMemsetAsync(B.status + kStatusDeferred, 0, 16, st);
         if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);

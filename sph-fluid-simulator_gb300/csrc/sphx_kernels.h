@@ -83,13 +83,12 @@ struct RowWarps {
 };
 
 // fr: 2 float4 per particle, (x, y, z, p) and (vx, vy, vz, 1/rho), written
-// by the density kernel when fr is set (vel then required).  With rw (and
-// T.rofs), each warp of the pass takes particles of one cell row only; else
-// consecutive threads take consecutive cell-sorted particles.
+// by the density kernel when fr is set (vel then required).  Each warp of
+// the pass takes particles of one cell row: T.rofs / T.rows describe the
+// rows and rw.wofs receives their warp offsets (rows + 1 entries).
 cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                            const float4 *vel, float4 *rp, float4 *fr, const NbrList &L,
-                           bool indirect, cudaStream_t st, int threads = 256,
-                           const RowWarps *rw = nullptr);
+                           bool indirect, cudaStream_t st, int threads, const RowWarps &rw);
 cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                          const float4 *vel, const float4 *rp, const float4 *fr, const NbrList &L,
                          float4 *pos_out, float4 *vel_out, float4 *force_out, bool indirect,

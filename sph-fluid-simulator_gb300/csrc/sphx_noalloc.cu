@@ -7,8 +7,9 @@
 // but does not let it call cudaMalloc (or any allocating routine) on its
 // behalf.  For them this entry point keeps every scratch buffer the density
 // pass needs (sort keys, ranks, cell order, the cell-grid counts and starts,
-// scan tile sums, the status word and the per-particle (rho, p, 1/rho)
-// record) in one file-scope __device__ array of fixed size.  The caller
+// scan tile sums, the status word, the per-row warp offsets and the
+// per-particle (rho, p, 1/rho) record) in one file-scope __device__ array of
+// fixed size.  The caller
 // passes the inputs (positions) and outputs (density, pressure) as device
 // pointers; nothing is allocated or freed, by this code or by a library it
 // calls.
@@ -61,8 +62,10 @@ constexpr size_t kOffRp = kOffTable + 1024;
 constexpr size_t kOffLarge = kOffRp + 16ull * kMaxParticles;  // queued large cells
 constexpr size_t kOffScat = kOffLarge + align256(8ull * (kMaxParticles / 64 + 2));
 constexpr size_t kOffDeferred = kOffScat + 8ull * kMaxParticles;
-constexpr size_t kScratchBytes = kOffDeferred + 4ull * kMaxParticles;
-static_assert(sizeof(sphx::StepParams) + 16 <= 1024, "scene table fits its scratch slot");
+constexpr uint32_t kRows = (uint32_t)kGridDim * kGridDim;  // cell rows of the grid
+constexpr size_t kOffRowWarps = kOffDeferred + align256(4ull * kMaxParticles);
+constexpr size_t kScratchBytes = kOffRowWarps + align256(4ull * (kRows + 1));
+static_assert(sizeof(sphx::StepParams) + 24 <= 1024, "scene table fits its scratch slot");
 
 static __device__ __align__(256) uint4 g_scratch[kScratchBytes / sizeof(uint4)];
 
@@ -160,17 +163,22 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     P.h2w = d.h * d.h * (1.0f + 3.814697265625e-06f);
     P.grid = sphx::Grid{kGridOrigin, kGridOrigin, kGridOrigin, kGridDim, kGridDim, kGridDim};
     P.n = (uint32_t)n;
-    // the one-scene table lives in the static array too: params, pofs {0, n}, sofs {0, slots}
+    // the one-scene table lives in the static array too: params, pofs {0, n},
+    // sofs {0, slots}, rofs {0, rows}
     struct {
         sphx::StepParams p;
         uint32_t pofs[2];
         uint32_t sofs[2];
-    } tbl = {P, {0u, (uint32_t)n}, {0u, kSlots}};
+        uint32_t rofs[2];
+    } tbl = {P, {0u, (uint32_t)n}, {0u, kSlots}, {0u, kRows}};
     char *dtbl = base + kOffTable;
-    const sphx::SceneTable T{reinterpret_cast<const sphx::StepParams *>(dtbl),
-                             reinterpret_cast<const uint32_t *>(dtbl + offsetof(decltype(tbl), pofs)),
-                             reinterpret_cast<const uint32_t *>(dtbl + offsetof(decltype(tbl), sofs)),
-                             1u, (uint32_t)n};
+    sphx::SceneTable T{reinterpret_cast<const sphx::StepParams *>(dtbl),
+                       reinterpret_cast<const uint32_t *>(dtbl + offsetof(decltype(tbl), pofs)),
+                       reinterpret_cast<const uint32_t *>(dtbl + offsetof(decltype(tbl), sofs)),
+                       1u, (uint32_t)n};
+    T.rofs = reinterpret_cast<const uint32_t *>(dtbl + offsetof(decltype(tbl), rofs));
+    T.rows = kRows;
+    const sphx::RowWarps RW{reinterpret_cast<uint32_t *>(base + kOffRowWarps)};
 
     sphx::SortBuffers B;
     B.key = reinterpret_cast<uint32_t *>(base + kOffKey);
@@ -197,7 +205,7 @@ extern "C" int sphx_density_static(const sphx_settings *s, const void *d_pos4, s
     SPHX_CUDA(cudaMemcpyAsync(dtbl, &tbl, sizeof tbl, cudaMemcpyHostToDevice, st));
     SPHX_CUDA(sphx::launch_sort(T, B, pos, st));
     SPHX_CUDA(sphx::launch_density(T, B, pos, nullptr, rp, nullptr, sphx::NbrList{nullptr, nullptr, 0},
-                                   /*indirect=*/true, st));
+                                   /*indirect=*/true, st, 128, RW));
     k_split_rho_prs<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(P.n, rp, d_rho, d_prs);
     SPHX_CUDA(cudaGetLastError());
 

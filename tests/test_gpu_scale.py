@@ -56,6 +56,14 @@ def one_step_vs_oracle(sphx, port, side, seed):
           % (len(pos), {f: "%.1e" % e for f, e in errs.items()}))
     for f in FIELDS:
         assert errs[f] < REL_TOL, f
+    # Both FP32 implementations against the FP64 evaluation of the same sums:
+    # the GPU's error may not exceed twice the reference's own.
+    rho64, prs64, f64 = port.fields_f64(pos, vel, CONFIG_ARGS)
+    for name, gpu, ref, exact in (("rho", out["rho"], r.rho, rho64), ("prs", out["prs"], r.prs, prs64),
+                                  ("force", out["force"], r.force, f64)):
+        e_gpu, e_ref = rel_err(gpu, exact), rel_err(ref, exact)
+        print("  %s: gpu-vs-f64 %.2e  ref-vs-f64 %.2e" % (name, e_gpu, e_ref))
+        assert e_gpu <= max(2 * e_ref, 1e-6), name
 
 
 def test_2m_one_step_fields_vs_oracle(sphx_lib, port):
