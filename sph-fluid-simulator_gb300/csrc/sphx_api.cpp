@@ -157,7 +157,7 @@ struct Layout {
     enum {
         kPos0, kPos1, kVel0, kVel1, kId0, kId1, kRp, kForce, kKey, kRank, kOrder, kCount,
         kStart, kTiles, kStatus, kStaging, kParams, kPofs, kSofs, kLarge, kFr, kNbr, kNcount,
-        kScat, kRofs, kRowOfs, kDeferred, kCflags, kBlkHdr, kNum
+        kScat, kRofs, kRowOfs, kDeferred, kCflags, kNum
     };
     size_t off[kNum];
     size_t total;
@@ -171,10 +171,8 @@ Layout layout_for(size_t cn, size_t cs, size_t csc, size_t slots) {
                                         sizeof(sphx::StepParams) * csc, 4 * (csc + 1),
                                         4 * (csc + 1), 8ull * sphx::large_list_cap((uint32_t)cn),
                                         32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn,
-                                        4 * (csc + 1), 4 * (cs + 1),
-                                        8 * cn + 16 * (size_t)sphx::row_blocks_cap((uint32_t)cn, (uint32_t)cs),
-                                        cs + 1,
-                                        8 * (size_t)sphx::row_blocks_cap((uint32_t)cn, (uint32_t)cs)};
+                                        4 * (csc + 1), 4 * (cs + 1), 8 * cn + 4 * (cn / 32 + 1),
+                                        cs + 1};
     Layout L;
     size_t o = 0;
     for (int k = 0; k < Layout::kNum; ++k) {
@@ -214,8 +212,7 @@ void bind(sphx_handle *h, char *a, const Layout &L) {
     h->nbr = (uint32_t *)(a + L.off[Layout::kNbr]);
     h->ncount = (uint32_t *)(a + L.off[Layout::kNcount]);
     h->d_rofs = (uint32_t *)(a + L.off[Layout::kRofs]);
-    h->row_warps = sphx::RowWarps{(uint32_t *)(a + L.off[Layout::kRowOfs]),
-                                  (uint2 *)(a + L.off[Layout::kBlkHdr])};
+    h->row_warps = sphx::RowWarps{(uint32_t *)(a + L.off[Layout::kRowOfs])};
 }
 
 // Allocates an arena for the capacities, zeroes its counts and status.
@@ -367,7 +364,7 @@ cudaError_t enqueue_step(sphx_handle *h, bool reorder, int &pv, int &idc, cudaEv
                                   st, h->tune.density_threads, h->row_warps)) != cudaSuccess)
         return e;
     if (ev) cudaEventRecord(ev[2], st);
-    if ((e = sphx::launch_force(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L, h->row_warps,
+    if ((e = sphx::launch_force(T, h->sb, h->pos[pv], h->vel[pv], h->rp, h->fr, L,
                                 h->pos[pv ^ 1], h->vel[pv ^ 1], h->force, !reorder, st,
                                 h->tune.force_threads)) != cudaSuccess)
         return e;

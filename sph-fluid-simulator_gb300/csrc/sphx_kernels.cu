@@ -909,14 +909,11 @@ __device__ __forceinline__ void warp_walk(const WalkCtx &W, const WalkStart &s, 
 
 // The cooperative walk shares a warp's loads among lanes of the same cell
 // row; a warp whose particles straddle two rows walks them as two groups,
-// one after the other, with half its lanes idle each time.  So the walk
-// passes give every warp the particles of one row only: row R's particles
-// [start[first], start[first + gx]) go to ceil(count / 128) row blocks of
-// four warps (32 particles each), numbered from wofs[R], an exclusive scan of
-// those warp counts over all rows (entry rows is the total).  Lanes past a
-// row's end idle; a row block's trailing warps may hold none.  The force
-// pass runs one CTA per row block and stages the block's neighbour records
-// in shared memory.
+// one after the other, with half its lanes idle each time.  So the density
+// pass gives every warp the particles of one row only: row R's particles
+// [start[first], start[first + gx]) go to ceil(count / 32) warps, numbered
+// from wofs[R], an exclusive scan of those counts over all rows (entry rows
+// is the total).  Lanes past a row's end idle.
 
 // Scene of global cell row R: the last s with rofs[s] <= R.
 __device__ __forceinline__ uint32_t scene_of_row(const SceneTable &T, uint32_t R) {
@@ -954,9 +951,10 @@ __device__ __forceinline__ uint32_t row_of_warp(const uint32_t *__restrict__ wof
     return lo;
 }
 
-// Threads a density launch needs: four warps per row block.
+// Threads a density launch needs: at most n / 32 + rows warps (each row's
+// last warp is partial).
 __host__ __forceinline__ uint32_t launch_threads(const SceneTable &T) {
-    return row_blocks_cap(T.n, T.rows) * 128u;
+    return (T.n / 32u + T.rows + 1u) * 32u;
 }
 
 // Kernel 1, kScanTile rows per block: every row's warp count, scanned within
@@ -976,8 +974,7 @@ __global__ void k_row_warps(SceneTable T, const uint32_t *__restrict__ start,
         if (R < T.rows && !err) {
             const uint32_t sc = scene_of_row(T, R);
             const uint32_t f = row_first_slot(T, sc, R);
-            // whole row blocks of four warps: ceil(count / 128) * 4
-            v[k] = ((start[f + (uint32_t)T.params[sc].grid.gx] - start[f] + 127u) >> 7) << 2;
+            v[k] = (start[f + (uint32_t)T.params[sc].grid.gx] - start[f] + 31u) >> 5;
         }
         s += v[k];
     }
@@ -1111,94 +1108,20 @@ __device__ __forceinline__ void density_finish(const StepParams &P, float acc, u
     }
 }
 
-// List count flags: no list recorded (the force pass walks for the
-// particle), and a list of 16-bit staged offsets (2 per slot).
-constexpr uint32_t kStagedList = 0x40000000u;
-constexpr uint32_t kCountMask = 0x3FFFFFFFu;
-
-// Whether the force pass walks for a particle with list count c: no list,
-// or more neighbours than its list holds.
-__device__ __forceinline__ bool list_overflows(uint32_t c, uint32_t slots) {
-    if (c & kNoList) return true;
-    return (c & kStagedList) ? (c & kCountMask) > 2u * slots : c > slots;
-}
-
-// Slot x of the particle at cell-sorted position p.
-__device__ __forceinline__ uint32_t slot_x(const StepParams &P, const WalkCtx &G, bool ind,
-                                           uint32_t p) {
-    const CellPos c = cell_pos(G.pos[ind ? G.order[p] : p], P.h);
-    int mx, my, mz;
-    slot_of(P.grid, c.cx, c.cy, c.cz, mx, my, mz);
-    return (uint32_t)mx;
-}
-
-// A row block's staged layout, warp-uniform: whether its lists are staged,
-// and in lane r < 9 the offset that turns a cell-sorted position of
-// neighbour row r into an index of the concatenation (the row's start in it
-// minus the row's first position).
-struct BlockStage {
-    bool staged;
-    uint32_t eoff;
-};
-
-// The layout of a warp's row block (every warp of the block computes the
-// same), recorded in RW.hdr by the block's first warp.  w: the warp, lw: its
-// index within the row, f: the row's first slot.  Staged when lists are
-// wanted, the block's slot x range keeps one cell off the grid's x seam on
-// either side and the nine runs together hold at most kForceStage particles.
-__device__ __forceinline__ BlockStage block_stage(const WalkCtx &W, const StepParams &P,
-                                                  const WalkCtx &G, bool ind, const RowWarps &RW,
-                                                  uint32_t w, uint32_t lw, uint32_t f, int my, int mz,
-                                                  bool lists) {
-    BlockStage bs{false, 0u};
-    if (!RW.hdr) return bs;
-    const uint32_t lane = threadIdx.x & 31u;
-    const Grid &g = W.grid;
-    const uint32_t gx = (uint32_t)g.gx;
-    // the block's particles [p0, p1): the row's 128-particle segment
-    const uint32_t R0 = W.start[f], R1 = W.start[f + gx];
-    const uint32_t p0 = R0 + ((lw >> 2) << 7), p1 = min(p0 + 128u, R1);
-    uint32_t x = 0u;
-    if (lane < 2) x = slot_x(P, G, ind, lane == 0 ? p0 : p1 - 1u);
-    const uint32_t bx0 = __shfl_sync(0xffffffffu, x, 0), bx1 = __shfl_sync(0xffffffffu, x, 1);
-    const bool ok = lists && bx0 >= 1u && bx1 + 1u < gx;
-    uint32_t A = 0u, len = 0u;
-    if (ok && lane < 9u) {
-        const int dz = (int)lane / 3 - 1, dy = (int)lane % 3 - 1;
-        const uint32_t base =
-            ((uint32_t)wrap1(mz + dz, g.gz) * (uint32_t)g.gy + (uint32_t)wrap1(my + dy, g.gy)) * gx;
-        A = W.start[base + bx0 - 1u];
-        len = W.start[base + bx1 + 2u] - A;
-    }
-    uint32_t incl = len;
-#pragma unroll
-    for (int d = 1; d < 16; d <<= 1) {
-        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= (uint32_t)d) incl += v;
-    }
-    const uint32_t total = __shfl_sync(0xffffffffu, incl, 8);
-    bs.staged = ok && total <= kForceStage;
-    bs.eoff = (incl - len) - A;
-    if ((w & 3u) == 0u && lane == 0u)
-        RW.hdr[w >> 2] = bs.staged ? make_uint2(bx0, bx1) : make_uint2(0xffffffffu, 0xffffffffu);
-    return bs;
-}
-
 // One lane's scan of chunk slots [lo, hi) of a neighbour row (the chunk
 // holds cell-sorted positions c0, c0 + 1, ...): every candidate inside the
 // lane's x window is tested with the reference's float r^2 (sph.cpp:57: (dx*dx
 // + dy*dy) + dz*dz, no fused multiply-add); an accepted one adds
 // (h^2 - r^2)^3 to the compensated sum and its index to the list row (while
-// it has room: a 16-bit staged offset with kStaged, see k_force).  x-sorted
-// runs (xmono): start at the first x >= xlo
+// it has room).  x-sorted runs (xmono): start at the first x >= xlo
 // (binary search), stop at the first x > xhi; returns true once past the
 // window.  Otherwise every slot is checked against the window.
-template <bool kInd, bool kStaged>
+template <bool kInd>
 __device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c0, uint32_t lo,
                                              uint32_t hi, float xlo, float xhi, bool xmono,
                                              float4 pi, float h2, uint32_t self, float &ks,
                                              float &kc, uint32_t &cnt, uint32_t *lrow,
-                                             uint32_t lcap, uint32_t eoff) {
+                                             uint32_t lcap) {
     auto visit = [&](uint32_t k, float4 p) {
         const float dx = __fsub_rn(p.x, pi.x);
         const float dy = __fsub_rn(p.y, pi.y);
@@ -1208,13 +1131,7 @@ __device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c
             kahan_add_cube(ks, kc, __fsub_rn(h2, d2));
             // streaming store: the force pass reads the row once, after
             // every other row has been written
-            if (cnt < lcap) {
-                if (kStaged)
-                    __stcs(reinterpret_cast<unsigned short *>(lrow) + cnt,
-                           (unsigned short)(eoff + c0 + k));
-                else
-                    __stcs(lrow + cnt, kInd ? sm.idx[k] : c0 + k);
-            }
+            if (cnt < lcap) __stcs(lrow + cnt, kInd ? sm.idx[k] : c0 + k);
             ++cnt;
         }
     };
@@ -1285,12 +1202,6 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     walk_start(W, P, pi, s);
     const bool fast = valid && s.flags == 0u && s.mx >= 1 && s.mx + 1 < g.gx;
     defer_lanes(valid && !fast, t, deferred, &status[kStatusDeferred]);
-    // The row block's staged form (see k_force): its particles' slot x range
-    // [bx0, bx1], the nine neighbour rows' runs over cells [bx0 - 1, bx1 + 1]
-    // concatenated in walk order.  If it fits kForceStage records, lists hold
-    // 16-bit offsets into that concatenation (`eoff` of a row + the cell-sorted
-    // position), else 32-bit particle indices.
-    const BlockStage bs = block_stage(W, P, G, kInd, RW, w, w - RW.wofs[R], f, my, mz, L.nbr != nullptr);
     if (!__any_sync(0xffffffffu, fast)) return;
     const uint32_t mxlo = __reduce_min_sync(0xffffffffu, fast ? (uint32_t)s.mx : 0xffffffffu);
     const uint32_t mxhi = __reduce_max_sync(0xffffffffu, fast ? (uint32_t)s.mx : 0u);
@@ -1300,7 +1211,7 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
     const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
     uint32_t *lrow = fast ? density_row(W, s, L, i) : nullptr;
-    const uint32_t lcap = lrow ? (bs.staged ? 2u * L.slots : L.slots) : 0u;
+    const uint32_t lcap = lrow ? L.slots : 0u;
     float ks = 0.f, kc = 0.f;
     uint32_t cnt = 0u;
     PosSmem<kInd> &sm = s_chunk[threadIdx.x >> 5];
@@ -1316,7 +1227,6 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
             if (!__any_sync(0xffffffffu, need)) continue;
             const uint32_t base = (zrow + (uint32_t)wrap1(my + dy, g.gy)) * gx;
             const uint32_t A = W.start[base + mxlo - 1], B = W.start[base + mxhi + 2];
-            const uint32_t eoff = __shfl_sync(0xffffffffu, bs.eoff, (dz + 1) * 3 + (dy + 1));
             uint32_t a = 0u, b = 0u;
             if (need) {
                 a = W.start[base + s.mx - 1];
@@ -1334,20 +1244,14 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
                     if (kInd) sm.idx[k] = j;
                 }
                 __syncwarp();
-                if (!done && b > c0 && a < c0 + m) {
-                    const uint32_t lo = a > c0 ? a - c0 : 0u, hi = min(b - c0, m);
-                    done = bs.staged
-                               ? density_scan<kInd, true>(sm, c0, lo, hi, xlo, xhi, W.xmono, pi, W.h2, t,
-                                                          ks, kc, cnt, lrow, lcap, eoff)
-                               : density_scan<kInd, false>(sm, c0, lo, hi, xlo, xhi, W.xmono, pi, W.h2,
-                                                           t, ks, kc, cnt, lrow, lcap, 0u);
-                }
+                if (!done && b > c0 && a < c0 + m)
+                    done = density_scan<kInd>(sm, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo, xhi,
+                                              W.xmono, pi, W.h2, t, ks, kc, cnt, lrow, lcap);
                 __syncwarp();
             }
         }
     }
-    if (fast) density_finish(P, ks, cnt | (bs.staged ? kStagedList : 0u), lrow != nullptr, i, pi, vel,
-                             rp, fr, L);
+    if (fast) density_finish(P, ks, cnt, lrow != nullptr, i, pi, vel, rp, fr, L);
 }
 
 // The particles k_density deferred, one warp each (warp_walk).
@@ -1571,164 +1475,69 @@ __device__ __forceinline__ void force_finish(const StepParams &P, const ForcePai
     vel_out[i] = v;
 }
 
-// The row, scene and particle of warp w of the walk passes (row warps):
-// warp-uniform row R, its scene and first slot, the lane's cell-sorted
-// position t and whether it holds a particle.
-struct RowLane {
-    uint32_t R, sc, f, t;
-    int my, mz;
-    bool valid;
-};
-
-__device__ __forceinline__ RowLane row_lane(const SceneTable &T, const WalkCtx &G, const RowWarps &RW,
-                                            uint32_t w) {
-    RowLane r;
-    r.R = row_of_warp(RW.wofs, T.rows, w);
-    r.sc = scene_of_row(T, r.R);
-    const Grid &g = T.params[r.sc].grid;
-    const uint32_t Rl = r.R - T.rofs[r.sc];  // my + gy * mz
-    r.my = (int)(Rl % (uint32_t)g.gy);
-    r.mz = (int)(Rl / (uint32_t)g.gy);
-    r.f = Rl * (uint32_t)g.gx;
-    const uint32_t *start = G.start + T.sofs[r.sc];
-    r.t = start[r.f] + ((w - RW.wofs[r.R]) << 5) + (threadIdx.x & 31u);
-    r.valid = r.t < start[r.f + (uint32_t)g.gx];
-    return r;
-}
-
 // Force of every particle whose neighbours fit its list (same neighbours,
-// same order as the density walk), then integration and walls; one CTA of
-// four warps per row block.  Where the density pass staged the block's lists
-// (RW.hdr), the CTA first copies the neighbour records of the nine runs over
-// cells [bx0 - 1, bx1 + 1] (concatenated in walk order, as block_stage laid
-// them out) into shared memory, and a list entry is an index into that copy:
-// every pair then reads its 32-byte record from shared memory instead of
-// gathering it from L2, which bounded this pass (one L1 wavefront per
-// gathered record).  Other lists hold particle indices and gather.  Either
-// way the pairs are summed in list order, so the bits do not depend on the
-// form.  Warps holding a particle past its list are listed for k_force_walk.
-template <bool kInd>
-__global__ void __launch_bounds__(128, 5)
+// same order as the density walk), then integration and walls.  The others
+// are k_force_walk's, which this kernel tells which warps (32 cell-sorted
+// particles) hold one: keeping the walk out of this kernel leaves it 48
+// registers instead of 64 with spills (0.257 against 0.276 ms at 2.1M).
+template <bool kInd, int kThreads>
+__global__ void __launch_bounds__(kThreads, kForceListThreadsPerSM / kThreads)
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
-            const float4 *__restrict__ fr, NbrList L, RowWarps RW, float4 *__restrict__ pos_out,
+            const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
             uint32_t *__restrict__ walk_warps, uint32_t *__restrict__ status) {
-    extern __shared__ float4 s_stage[];  // kForceStage records: (x, y, z, p), (vx, vy, vz, 1/rho)
-    __shared__ uint32_t s_run[28];       // per neighbour row: first position, length, offset; bad
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (status[0] & kStatusErrorMask) return;
-    const uint32_t lane = threadIdx.x & 31u;
-    if ((blockIdx.x << 2) >= RW.wofs[T.rows]) return;  // whole CTA
-    const uint32_t w = (blockIdx.x << 2) + (threadIdx.x >> 5);
-    const RowLane rl = row_lane(T, G, RW, w);  // the four warps share the row
-    const uint2 hh = RW.hdr[blockIdx.x];
-    if (hh.x != 0xffffffffu) {  // CTA-uniform
-        if (threadIdx.x < 9u) {
-            const Grid &g = T.params[rl.sc].grid;
-            const uint32_t *start = G.start + T.sofs[rl.sc];
-            const int dz = (int)threadIdx.x / 3 - 1, dy = (int)threadIdx.x % 3 - 1;
-            const uint32_t base = ((uint32_t)wrap1(rl.mz + dz, g.gz) * (uint32_t)g.gy +
-                                   (uint32_t)wrap1(rl.my + dy, g.gy)) * (uint32_t)g.gx;
-            const uint32_t A = start[base + hh.x - 1u];
-            s_run[threadIdx.x] = A;
-            s_run[9 + threadIdx.x] = start[base + hh.y + 2u] - A;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t o = 0;
-            for (int r = 0; r < 9; ++r) {
-                s_run[18 + r] = o;
-                o += s_run[9 + r];
-            }
-            // block_stage admitted this layout; a larger one would mean the
-            // runs changed since the density pass: report it, stage nothing
-            s_run[27] = o > kForceStage;
-            if (o > kForceStage) atomicOr(status, kStatusOverflowBit);
-        }
-        __syncthreads();
-        if (s_run[27]) return;  // CTA-uniform
-#pragma unroll 1
-        for (int r = 0; r < 9; ++r) {
-            const uint32_t A = s_run[r], n = s_run[9 + r], o = s_run[18 + r];
-            for (uint32_t k = threadIdx.x; k < n; k += 128u) {
-                const uint32_t j = kInd ? G.order[A + k] : A + k;
-                float4 a, b;
-                load_record(fr, j, a, b);
-                s_stage[2 * (o + k)] = a;
-                s_stage[2 * (o + k) + 1] = b;
-            }
-        }
-        __syncthreads();
-    }
-    const uint32_t i = rl.valid ? (kInd ? G.order[rl.t] : rl.t) : 0u;
-    const uint32_t c = rl.valid ? L.count[i] : 0u;
-    const bool walker = rl.valid && list_overflows(c, L.slots);
-    if (__ballot_sync(0xffffffffu, walker) && lane == 0)
-        walk_warps[atomicAdd(&status[kStatusWalkWarps], 1u)] = w;
-    if (!rl.valid || walker) return;
-    const StepParams &P = T.params[rl.sc];
+    const bool valid = t < T.n;  // the grid is whole blocks: every lane gets here
+    const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
+    const uint32_t cnt = valid ? L.count[i] : 0u;
+    const uint32_t wm = __ballot_sync(0xffffffffu, valid && cnt > L.slots);
+    if (wm && (threadIdx.x & 31u) == (uint32_t)(__ffs(wm) - 1))
+        walk_warps[atomicAdd(&status[kStatusWalkWarps], 1u)] = t >> 5;
+    if (!valid || cnt > L.slots) return;
+    const uint32_t sc = scene_of(T, i);
+    const StepParams &P = T.params[sc];
     const float4 pi = G.pos[i];
     const float4 vi = vel[i];
     const float4 q = rp[i];
     ForcePair pair{vi, q.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const uint32_t cnt = c & kCountMask;
-    // rows are 16-byte aligned (slots is a multiple of 4); entries past cnt in
-    // the last load are never used
+    // the row is 16-byte aligned (slots is a multiple of 4): four entries per
+    // load; entries past cnt in the last load are never used
     const uint4 *row = reinterpret_cast<const uint4 *>(L.nbr + (size_t)i * L.slots);
-    if (c & kStagedList) {
-        // eight 16-bit entries per load, two records in flight
 #pragma unroll 1
-        for (uint32_t k = 0; k < cnt; k += 8) {
-            const uint4 e = row[k >> 3];
-            const uint32_t left = cnt - k;
-            const uint32_t ew[4] = {e.x, e.y, e.z, e.w};
-#pragma unroll
-            for (int h2 = 0; h2 < 4; ++h2) {
-                if ((uint32_t)(2 * h2) < left) {
-                    const uint32_t j0 = ew[h2] & 0xFFFFu;
-                    const uint32_t j1 = (uint32_t)(2 * h2 + 1) < left ? ew[h2] >> 16 : j0;
-                    const float4 a0 = s_stage[2 * j0], b0 = s_stage[2 * j0 + 1];
-                    const float4 a1 = s_stage[2 * j1], b1 = s_stage[2 * j1 + 1];
-                    pair_add_record(pair, a0, b0, pi);
-                    if ((uint32_t)(2 * h2 + 1) < left) pair_add_record(pair, a1, b1, pi);
-                }
-            }
+    for (uint32_t k = 0; k < cnt; k += 4) {
+        const uint4 e = row[k >> 2];
+        const uint32_t left = cnt - k;
+        {  // two records in flight, then summed in list order
+            const uint32_t j1 = left > 1 ? e.y : e.x;
+            float4 a0, b0, a1, b1;
+            load_record(fr, e.x, a0, b0);
+            load_record(fr, j1, a1, b1);
+            pair_add_record(pair, a0, b0, pi);
+            if (left > 1) pair_add_record(pair, a1, b1, pi);
         }
-    } else {
-#pragma unroll 1
-        for (uint32_t k = 0; k < cnt; k += 4) {
-            const uint4 e = row[k >> 2];
-            const uint32_t left = cnt - k;
-            {  // two records in flight, then summed in list order
-                const uint32_t j1 = left > 1 ? e.y : e.x;
-                float4 a0, b0, a1, b1;
-                load_record(fr, e.x, a0, b0);
-                load_record(fr, j1, a1, b1);
-                pair_add_record(pair, a0, b0, pi);
-                if (left > 1) pair_add_record(pair, a1, b1, pi);
-            }
-            if (left > 2) {
-                const uint32_t j3 = left > 3 ? e.w : e.z;
-                float4 a2, b2, a3, b3;
-                load_record(fr, e.z, a2, b2);
-                load_record(fr, j3, a3, b3);
-                pair_add_record(pair, a2, b2, pi);
-                if (left > 3) pair_add_record(pair, a3, b3, pi);
-            }
+        if (left > 2) {
+            const uint32_t j3 = left > 3 ? e.w : e.z;
+            float4 a2, b2, a3, b3;
+            load_record(fr, e.z, a2, b2);
+            load_record(fr, j3, a3, b3);
+            pair_add_record(pair, a2, b2, pi);
+            if (left > 3) pair_add_record(pair, a3, b3, pi);
         }
     }
     force_finish(P, pair, i, pi, vi, q.x, pos_out, vel_out, force_out);
 }
 
-// Force of the particles past their list (clumped fluid), over the row
-// warps k_force listed: a warp-cooperative walk over the neighbour records
-// in the density walk's order, the whole warp loading for its walking lanes.
+// Force of the particles past their list (clumped fluid), over the warps
+// k_force listed: a warp-cooperative walk over the neighbour records in the
+// density walk's order, the whole warp loading for its walking lanes.
 // Walkers off the cooperative path (bucket collision, grid seam) are listed
 // in `deferred` for k_force_deferred.
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, kForceThreadsPerSM / kThreads)
     k_force_walk(SceneTable T, WalkCtx G, const float4 *__restrict__ vel,
                  const float4 *__restrict__ rp, const float4 *__restrict__ fr, NbrList L,
-                 RowWarps RW, float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
+                 float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
                  float4 *__restrict__ force_out, const uint32_t *__restrict__ walk_warps,
                  uint32_t *__restrict__ deferred, uint32_t *__restrict__ status) {
     __shared__ RecordSmem<kInd> s_coop[kThreads / 32];
@@ -1744,12 +1553,11 @@ __global__ void __launch_bounds__(kThreads, kForceThreadsPerSM / kThreads)
         if (lane == 0) q = atomicAdd(&status[kStatusWalkNext], 1u);
         q = __shfl_sync(0xffffffffu, q, 0);
         if (q >= m) break;
-        const RowLane rl = row_lane(T, G, RW, walk_warps[q]);
-        const uint32_t t = rl.t;
-        const bool valid = rl.valid;
+        const uint32_t t = walk_warps[q] * 32u + lane;
+        const bool valid = t < T.n;
         const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
-        const bool walker = valid && list_overflows(L.count[i], L.slots);
-        const uint32_t sc = rl.sc;
+        const bool walker = valid && L.count[i] > L.slots;
+        const uint32_t sc = valid ? scene_of(T, i) : 0u;
         const StepParams &P = T.params[sc];
         const float4 pi = G.pos[i];
         const float4 vi = vel[i];
@@ -2066,10 +1874,11 @@ cudaError_t launch_cell_flags(const SceneTable &T, uint32_t slots, uint8_t *cfla
     return cudaGetLastError();
 }
 
-// The force kernel stages kForceStage records (45 KB) per CTA: five CTAs
-// per SM need the whole shared-memory carveout.
-constexpr int kForceCarveout = 100;
-constexpr size_t kForceStageBytes = (size_t)kForceStage * 32u;
+// The force list kernel uses no shared memory and is bound by L1 throughput
+// on the neighbour records: all of the SM's L1 as cache (carveout 0) took it
+// from 0.268 to 0.261 ms at 2.1M particles.  The density kernel gained
+// nothing either way (it keeps the driver's choice).
+constexpr int kForceCarveout = 0;
 
 // Preferred shared-memory share of an SM's L1 for a kernel (percent of the
 // maximum; -1 leaves the driver's choice).
@@ -2083,14 +1892,10 @@ static cudaError_t carveout(K *kernel, int percent) {
 cudaError_t prepare_device() {
     cudaError_t e = cudaFuncSetAttribute(k_cellsort_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          8 * kLargeCell);
-    if (e == cudaSuccess) e = carveout(k_force<false>, kForceCarveout);
-    if (e == cudaSuccess) e = carveout(k_force<true>, kForceCarveout);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_force<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kForceStageBytes);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_force<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kForceStageBytes);
+    if (e == cudaSuccess) e = carveout(k_force<false, 128>, kForceCarveout);
+    if (e == cudaSuccess) e = carveout(k_force<true, 128>, kForceCarveout);
+    if (e == cudaSuccess) e = carveout(k_force<false, 256>, kForceCarveout);
+    if (e == cudaSuccess) e = carveout(k_force<true, 256>, kForceCarveout);
     return e;
 }
 
@@ -2148,46 +1953,44 @@ cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const floa
     return cudaGetLastError();
 }
 
-template <bool kInd, int kThreads>
+template <int kThreads>
 static void force_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel,
-                         const float4 *rp, const float4 *fr, const NbrList &L, const RowWarps &RW,
-                         float4 *pos_out, float4 *vel_out, float4 *force_out, uint32_t *deferred,
-                         uint32_t *walk_warps, uint32_t *status, cudaStream_t st) {
-    // one CTA per row block
-    k_force<kInd><<<row_blocks_cap(T.n, T.rows), 128, kForceStageBytes, st>>>(
-        T, G, vel, rp, fr, L, RW, pos_out, vel_out, force_out, walk_warps, status);
+                         const float4 *rp, const float4 *fr, const NbrList &L, float4 *pos_out,
+                         float4 *vel_out, float4 *force_out, bool indirect,
+                         uint32_t *deferred, uint32_t *walk_warps, uint32_t *status,
+                         cudaStream_t st) {
     // the walkers' kernel: as many warps as the GPU holds at once (or fewer)
     const unsigned walk_blocks =
         std::min<unsigned>(blocks(T.n, kThreads), 152u * (kForceThreadsPerSM / kThreads));
-    k_force_walk<kInd, kThreads><<<walk_blocks, kThreads, 0, st>>>(
-        T, G, vel, rp, fr, L, RW, pos_out, vel_out, force_out, walk_warps, deferred, status);
-    k_force_deferred<kInd><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
-        T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    if (indirect) {
+        k_force<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);
+        k_force_walk<true, kThreads><<<walk_blocks, kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, deferred, status);
+        k_force_deferred<true><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    } else {
+        k_force<false, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);
+        k_force_walk<false, kThreads><<<walk_blocks, kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, deferred, status);
+        k_force_deferred<false><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    }
 }
 
 cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                          const float4 *vel, const float4 *rp, const float4 *fr, const NbrList &L,
-                         const RowWarps &RW, float4 *pos_out, float4 *vel_out, float4 *force_out,
-                         bool indirect, cudaStream_t st, int threads) {
-    if (!T.rofs || !T.rows || !RW.wofs || !RW.hdr) return cudaErrorInvalidValue;
+                         float4 *pos_out, float4 *vel_out, float4 *force_out, bool indirect,
+                         cudaStream_t st, int threads) {
     const WalkCtx G = global_ctx(B, pos);
     if (T.n) {
-        uint32_t *def = B.deferred + T.n, *ww = B.deferred + 2 * (size_t)T.n;
-        if (indirect) {
-            if (threads == 128)
-                force_launch<true, 128>(T, G, vel, rp, fr, L, RW, pos_out, vel_out, force_out, def, ww,
-                                        B.status, st);
-            else
-                force_launch<true, 256>(T, G, vel, rp, fr, L, RW, pos_out, vel_out, force_out, def, ww,
-                                        B.status, st);
-        } else {
-            if (threads == 128)
-                force_launch<false, 128>(T, G, vel, rp, fr, L, RW, pos_out, vel_out, force_out, def,
-                                         ww, B.status, st);
-            else
-                force_launch<false, 256>(T, G, vel, rp, fr, L, RW, pos_out, vel_out, force_out, def,
-                                         ww, B.status, st);
-        }
+        if (threads == 128)
+            force_launch<128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
+                              B.deferred + T.n, B.deferred + 2 * (size_t)T.n, B.status, st);
+        else
+            force_launch<256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
+                              B.deferred + T.n, B.deferred + 2 * (size_t)T.n, B.status, st);
     }
     return cudaGetLastError();
 }

@@ -23,10 +23,9 @@ struct SortBuffers {
     uint32_t *status;    // 2 words: error bits, x-wrap flag (see below)
     uint2 *large;        // cells longer than 64 queued for the block sort
     const uint8_t *cflags;  // slots: collision flags of each slot's own cell, or NULL
-    uint32_t *deferred;  // 2n + 4 row_blocks_cap: cell-sorted positions of the particles
-                         // the density pass (first n) and the force pass (next n)
-                         // defer, then the row warps of the force pass that hold a
-                         // walker
+    uint32_t *deferred;  // 2n + n / 32 + 1: cell-sorted positions of the particles the
+                         // density pass (first n) and the force pass (next n) defer,
+                         // then the warps of the force pass that hold a walker
     uint32_t large_cap;  // entries of `large` (n / 64 + 2 suffices)
     uint32_t slots;      // gx * gy * gz
     uint32_t max_cell;   // occupancy above which a step refuses to walk (<= kLargeCell)
@@ -77,23 +76,11 @@ struct NbrList {
 };
 constexpr uint32_t kNbrSlotsDefault = 256, kNbrSlotsMax = 1024;
 
-// The walk passes' warps, each inside one cell row (see k_row_warps): every
-// row gets whole row blocks of four warps (128 particles), so warps 4b..4b+3
-// are row block b.  wofs[R] = first warp of cell row R (a multiple of 4),
-// rows + 1 entries.  hdr[b] = the slot x range (first, last) of row block b's
-// particles when the density pass wrote its lists in the staged (16-bit)
-// form, else (~0, ~0); NULL: nothing staged (no force pass follows).
+// The density pass's warps, each inside one cell row (see k_row_warps):
+// wofs[R] = first warp of cell row R, rows + 1 entries.
 struct RowWarps {
     uint32_t *wofs;
-    uint2 *hdr = nullptr;
 };
-// Upper bound on the row blocks of a step: rows hold ceil(count / 128)
-// blocks each, so at most n / 128 + (non-empty rows) blocks.
-inline uint32_t row_blocks_cap(uint32_t n, uint32_t rows) {
-    return n / 128u + (rows < n ? rows : n) + 1u;
-}
-// Records a force block stages in shared memory (45 KB: five blocks per SM).
-constexpr uint32_t kForceStage = 1408;
 
 // fr: 2 float4 per particle, (x, y, z, p) and (vx, vy, vz, 1/rho), written
 // by the density kernel when fr is set (vel then required).  Each warp of
@@ -102,14 +89,10 @@ constexpr uint32_t kForceStage = 1408;
 cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                            const float4 *vel, float4 *rp, float4 *fr, const NbrList &L,
                            bool indirect, cudaStream_t st, int threads, const RowWarps &rw);
-// The force pass over the density pass's lists: one CTA per row block of
-// rw (the same row blocks and rw.hdr the density pass used), the walkers of
-// particles past their list, the deferred ones.  `threads` is the walkers'
-// block size.
 cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                          const float4 *vel, const float4 *rp, const float4 *fr, const NbrList &L,
-                         const RowWarps &rw, float4 *pos_out, float4 *vel_out, float4 *force_out,
-                         bool indirect, cudaStream_t st, int threads);
+                         float4 *pos_out, float4 *vel_out, float4 *force_out, bool indirect,
+                         cudaStream_t st, int threads = 256);
 // Per particle (scene offset + id): accepted neighbour visits, their id
 // fingerprint and, if tests is set, the candidates whose r^2 was evaluated.
 cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float4 *pos,
