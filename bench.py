@@ -376,6 +376,28 @@ SIDE_8M = 200  # 200^3 = 8,000,000 particles
 REORDER_SWEEP = (1, 4, 16, 64)
 
 
+def copy_ceiling(torch, nbytes, reps=10):
+    """Single-copy rates (GB/s) between pinned host memory and the device, each
+    direction alone, for copies of nbytes."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for kind in ("h2d", "d2h"):
+        for _ in range(2):
+            (d.copy_(h, non_blocking=True) if kind == "h2d" else h.copy_(d, non_blocking=True))
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            (d.copy_(h, non_blocking=True) if kind == "h2d" else h.copy_(d, non_blocking=True))
+        e1.record()
+        torch.cuda.synchronize()
+        out[kind + "_gbs"] = nbytes * reps / (e0.elapsed_time(e1) / 1e3) / 1e9
+    out["bytes"] = nbytes
+    return out
+
+
 def configured_run(sphx, torch, s, box, pos, device, steps, reorder, phases, peak):
     """`steps` steps from the initial lattice as CUDA-graph replays, timed with
     CUDA events on the scene's stream.  With `phases`, the same run again as
@@ -482,32 +504,51 @@ def run_sphx(a):
                                 OPS_PER_PAIR_DENSITY, OPS_PER_PAIR_FORCE)}
     sc.set_profiling(False)
 
-    # e2e through the C-ABI with pinned host buffers
+    # e2e through the C-ABI with pinned host buffers: every step uploads the
+    # state, steps (graph replay, as a user's handle does) and reads
+    # positions and velocities back.  The state is the window's last one.
     pin_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
     pin_vel = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
     st = sc.read()
     pin_pos[:] = st["pos"]
     pin_vel[:] = st["vel"]
+    sc.close()
+    sc = sphx.Scene(s, box, pin_pos, pin_vel,
+                    sphx.default_options(device=device, reorder_interval=a.reorder, use_graph=1))
     e2e_steps = max(1, min(a.steps, 10))
-    for _ in range(2):
+    lib = sphx.lib()
+
+    def e2e_iteration():
+        t0 = time.perf_counter()
         sc.set_state(pin_pos, pin_vel)
+        t1 = time.perf_counter()
         sc.step(sphx.DT, 1)
-        sphx._check(sphx.lib().sphx_read_state(sc.h, sphx._ptr(pin_pos), sphx._ptr(pin_vel),
-                                               None, None, None))
+        sphx._check(lib.sphx_read_state(sc.h, sphx._ptr(pin_pos), sphx._ptr(pin_vel), None, None,
+                                        None))
+        return t1 - t0, time.perf_counter() - t1
+
+    for _ in range(3):
+        e2e_iteration()
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        sc.set_state(pin_pos, pin_vel)
-        sc.step(sphx.DT, 1)
-        sphx._check(sphx.lib().sphx_read_state(sc.h, sphx._ptr(pin_pos), sphx._ptr(pin_vel),
-                                               None, None, None))
+    parts = [e2e_iteration() for _ in range(e2e_steps)]
     t_e2e = time.perf_counter() - t0
     barrier()
     t_e2e = max_over_ranks(t_e2e)
+    sc.close()
+    ceil = copy_ceiling(torch, 24 * n)
+    step_ms = ms / a.steps
+    copy_ms = 1e3 * 24 * n * (1.0 / ceil["h2d_gbs"] + 1.0 / ceil["d2h_gbs"]) / 1e9
     e2e = {"value": n * e2e_steps * world / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
-           "path": "sphx_set_state + sphx_step + sphx_read_state (pinned host buffers)"}
-    sc.close()
+           "ms_per_step": 1e3 * t_e2e / e2e_steps,
+           "upload_ms": 1e3 * float(np.mean([p[0] for p in parts])),
+           "step_and_readout_ms": 1e3 * float(np.mean([p[1] for p in parts])),
+           "copy_ceiling": ceil,
+           "bound_ms": step_ms + copy_ms,
+           "bound_note": "device step of the timed window + 24 B/particle each way at the measured "
+                         "single-copy pinned rates",
+           "path": "sphx_set_state + sphx_step (graph replay) + sphx_read_state (pinned host buffers)"}
 
     # The configured runs (200 steps from the initial lattice): the fluid
     # clumps as it falls (the reference's physics at these constants), so
