@@ -290,7 +290,7 @@ def serve_sweep(sphx, count, rates, tick, device):
             st = srv.stats()
         lat = np.array([x.done_s - x.submit_s for x in sts])
         span = max(x.done_s for x in sts) - min(x.submit_s for x in sts)
-        results.append({"rate_per_s": lam,
+        results.append({"rate_per_s": lam, "span_s": span,
                         "served": {"scenes_per_s": len(reqs) / span, "p50_s": q(lat, 50),
                                    "p95_s": q(lat, 95), "p99_s": q(lat, 99),
                                    "relayouts": int(st.relayouts), "ticks": int(st.ticks)},
@@ -300,6 +300,11 @@ def serve_sweep(sphx, count, rates, tick, device):
     n_ps = sum(len(p) * k for _, p, _, k in reqs)
     return {"requests": len(reqs), "particle_steps": n_ps, "steps_per_tick": tick,
             "hbm_budget_gb": 150, "rates": results,
+            # no schedule can finish the stream before its longest request
+            # finishes alone: the served span's floor
+            "longest_request_alone_s": float(max(service)),
+            "sequential_total_s": float(sum(service)),
+            "speedup_bound": float(sum(service)) / float(max(service)),
             "workload": "requests: N log-uniform [2000, 500000], steps U[100, 2000], k U[10,40], "
                         "mu U[0.5,3], dam-break blocks; sequential arm: each request alone through "
                         "the plain path (create, steps, readout), FIFO over the same arrivals"}

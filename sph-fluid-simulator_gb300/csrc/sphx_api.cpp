@@ -267,14 +267,14 @@ int upload_tables(sphx_handle *h) {
 // Uploads one scene's host state into rows [first, first + n) of buffer
 // parity (pv, idc), with scene-local ids.
 int upload_scene(sphx_handle *h, const sphx::Scene &sc, const float *pos3, const float *vel3,
-                 int pv, int idc, uint32_t *bad = nullptr) {
+                 int pv, int idc, uint32_t *bad = nullptr, bool keep_order = false) {
     const size_t n = sc.n;
     float *sp = h->staging, *sv = h->staging + 3 * (size_t)h->cap_n;
     SPHX_CUDA(cudaMemcpyAsync(sp, pos3, 12 * n, cudaMemcpyHostToDevice, h->stream));
     if (vel3) SPHX_CUDA(cudaMemcpyAsync(sv, vel3, 12 * n, cudaMemcpyHostToDevice, h->stream));
     else SPHX_CUDA(cudaMemsetAsync(sv, 0, 12 * n, h->stream));
     SPHX_CUDA(sphx::launch_upload_rows(sc.first, sc.n, sp, sv, h->pos[pv], h->vel[pv], h->id[idc],
-                                       sc.d.h, bad, h->stream));
+                                       sc.d.h, bad, keep_order, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));  // staging is reused by the next scene
     return SPHX_OK;
 }
@@ -803,9 +803,11 @@ int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3) {
     // first offending row, or stays all ones
     uint32_t *bad = h->sb.status + 3;
     SPHX_CUDA(cudaMemsetAsync(bad, 0xFF, 4, h->stream));
+    // rows keep their particles: the storage stays in the last step's cell
+    // order, which the next step's sort then finds already sorted
     for (const sphx::Scene &sc : h->scenes) {
         const int rc = upload_scene(h, sc, pos3 + 3ull * sc.first,
-                                    vel3 ? vel3 + 3ull * sc.first : nullptr, h->pv, h->idc, bad);
+                                    vel3 ? vel3 + 3ull * sc.first : nullptr, h->pv, h->idc, bad, true);
         if (rc) return rc;
     }
     SPHX_CUDA(cudaMemsetAsync(h->sb.status, 0, 8, h->stream));

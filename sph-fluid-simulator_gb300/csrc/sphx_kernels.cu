@@ -1657,26 +1657,30 @@ __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ i
 }
 
 // Rows [first, first + n) from host-ordered staging arrays (vel3 all zero
-// or uploaded); ids are scene-local: row - first.
+// or uploaded).  Without keep_order, row first + i takes particle i and its
+// id becomes i (scene-local).  With keep_order, every row keeps its particle
+// (id[row]) and takes that particle's values: the storage stays in the cell
+// order of the last step, so the next step's sort and gather find it sorted.
 // With `bad` set, a position that is non-finite or whose cell quotient x / h
 // is 2^30 or more in magnitude (the host check of a new scene, done here for
-// state replacements) lowers *bad to its row.
+// state replacements) lowers *bad to first + its particle index.
 __global__ void k_upload_rows(uint32_t first, uint32_t n, const float *__restrict__ pos3,
                               const float *__restrict__ vel3, float4 *__restrict__ pos,
                               float4 *__restrict__ vel, uint32_t *__restrict__ id, float h,
-                              uint32_t *__restrict__ bad) {
+                              uint32_t *__restrict__ bad, bool keep_order) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t r = first + i;
-    const float x = pos3[3 * i], y = pos3[3 * i + 1], z = pos3[3 * i + 2];
+    const uint32_t d = keep_order ? id[r] : i;  // the particle (index into the staging arrays)
+    const float x = pos3[3 * d], y = pos3[3 * d + 1], z = pos3[3 * d + 2];
     if (bad) {
         const bool ok = in_domain(__fdiv_rn(x, h)) && in_domain(__fdiv_rn(y, h)) &&
                         in_domain(__fdiv_rn(z, h));  // NaN and inf fail the bound too
-        if (!ok) atomicMin(bad, r);
+        if (!ok) atomicMin(bad, first + d);
     }
     pos[r] = make_float4(x, y, z, 0.f);
-    vel[r] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.f);
-    id[r] = i;
+    vel[r] = make_float4(vel3[3 * d], vel3[3 * d + 1], vel3[3 * d + 2], 0.f);
+    if (!keep_order) id[r] = i;
 }
 
 // The dam-break lattice of sphx_lattice (host, sphx_host.cpp) generated in
@@ -2012,8 +2016,10 @@ cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float
 
 cudaError_t launch_upload_rows(uint32_t first, uint32_t n, const float *pos3, const float *vel3,
                                float4 *pos, float4 *vel, uint32_t *id, float h, uint32_t *bad,
-                               cudaStream_t st) {
-    if (n) k_upload_rows<<<blocks(n, 256), 256, 0, st>>>(first, n, pos3, vel3, pos, vel, id, h, bad);
+                               bool keep_order, cudaStream_t st) {
+    if (n)
+        k_upload_rows<<<blocks(n, 256), 256, 0, st>>>(first, n, pos3, vel3, pos, vel, id, h, bad,
+                                                      keep_order);
     return cudaGetLastError();
 }
 

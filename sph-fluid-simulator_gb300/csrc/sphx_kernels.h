@@ -101,11 +101,12 @@ cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float
 // Rows [first, first + n) from host-ordered staging (scene-local ids), and
 // back: one scene's rows to staging in its id order (field: 0 pos, 1 vel,
 // 2 force, 3 rho, 4 prs).
-// bad: NULL, or a device word lowered to the first row whose position is
-// outside the walk's domain for cell size h (see k_upload_rows).
+// bad: NULL, or a device word lowered to first + the index of the first
+// particle whose position is outside the walk's domain for cell size h.
+// keep_order: rows keep their particles (id unchanged), see k_upload_rows.
 cudaError_t launch_upload_rows(uint32_t first, uint32_t n, const float *pos3, const float *vel3,
                                float4 *pos, float4 *vel, uint32_t *id, float h, uint32_t *bad,
-                               cudaStream_t st);
+                               bool keep_order, cudaStream_t st);
 // Dam-break lattice generated on the device into rows [first, first + n).
 struct LatticeGen {
     uint32_t nx, ny, nz;
