@@ -802,12 +802,18 @@ int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3) {
     // the domain check runs in the upload kernel: status word 3 ends as the
     // first offending row, or stays all ones
     uint32_t *bad = h->sb.status + 3;
+    // Rows keep their particles, so that the storage stays in the last
+    // step's cell order, which the next step's sort then finds sorted; but
+    // only while every step so far completed: a step that stopped on an
+    // error did not move the ids with the data, and the state is then
+    // rewritten in id order instead.
+    SPHX_CUDA(cudaMemcpyAsync(h->h_status, h->sb.status, 4, cudaMemcpyDeviceToHost, h->stream));
+    SPHX_CUDA(cudaStreamSynchronize(h->stream));
+    const bool keep = h->error == 0 && (*h->h_status & sphx::kStatusErrorMask) == 0;
     SPHX_CUDA(cudaMemsetAsync(bad, 0xFF, 4, h->stream));
-    // rows keep their particles: the storage stays in the last step's cell
-    // order, which the next step's sort then finds already sorted
     for (const sphx::Scene &sc : h->scenes) {
         const int rc = upload_scene(h, sc, pos3 + 3ull * sc.first,
-                                    vel3 ? vel3 + 3ull * sc.first : nullptr, h->pv, h->idc, bad, true);
+                                    vel3 ? vel3 + 3ull * sc.first : nullptr, h->pv, h->idc, bad, keep);
         if (rc) return rc;
     }
     SPHX_CUDA(cudaMemsetAsync(h->sb.status, 0, 8, h->stream));

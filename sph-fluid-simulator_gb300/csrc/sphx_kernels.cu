@@ -1671,7 +1671,13 @@ __global__ void k_upload_rows(uint32_t first, uint32_t n, const float *__restric
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t r = first + i;
-    const uint32_t d = keep_order ? id[r] : i;  // the particle (index into the staging arrays)
+    // the particle (index into the staging arrays); an id outside the scene
+    // (never, while the ids are a permutation) falls back to the row's index
+    uint32_t d = i;
+    if (keep_order) {
+        const uint32_t k = id[r];
+        d = k < n ? k : i;
+    }
     const float x = pos3[3 * d], y = pos3[3 * d + 1], z = pos3[3 * d + 2];
     if (bad) {
         const bool ok = in_domain(__fdiv_rn(x, h)) && in_domain(__fdiv_rn(y, h)) &&
