@@ -236,7 +236,7 @@ int sphx_update_particles_release(void);
  * device memory when they need the result (a plugin inside a frame with a
  * fixed GPU memory budget, or a host that gives the library buffers but no
  * right to call cudaMalloc).  Its scratch is one static device array of about
- * 8.6 MiB per GPU, held until the process exits; n may be at most 131,072
+ * 7 MiB per GPU, held until the process exits; n may be at most 131,072
  * (larger n: SPHX_ERR_INVALID).  Calls share that array, so calls whose work
  * overlaps on the GPU race.  It synchronises `stream` and reads a status
  * word back, so it cannot be called while that stream is being captured into

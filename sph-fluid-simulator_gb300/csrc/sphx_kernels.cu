@@ -1069,9 +1069,6 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
 // in fluid (none in the dam-break block), at most n.
 constexpr int kDeferredThreads = 128;
 constexpr unsigned kDeferredBlocks = 2 * 152;
-// Blocks of the crowded-cell kernels: eight per SM, each warp looping over
-// the listed particles.
-constexpr unsigned kDenseBlocks = 8 * 152;
 // No list is recorded for a particle whose cell holds more than
 // slots / kListSkipFactor particles; its count then carries kNoList.
 constexpr uint32_t kListSkipFactor = 4;
@@ -1109,19 +1106,6 @@ __device__ __forceinline__ void density_finish(const StepParams &P, float acc, u
         fr[2 * (size_t)i] = make_float4(pi.x, pi.y, pi.z, prs);
         fr[2 * (size_t)i + 1] = make_float4(vi.x, vi.y, vi.z, inv);
     }
-}
-
-// Particles of cells holding more than kDenseCell particles take the
-// crowded-cell path (k_density_dense, k_force_dense; see there), marked in
-// their list count by kDenseBit.
-constexpr uint32_t kDenseCell = kSmallCell;
-// List count flag of a crowded-cell particle: no list, force by k_force_dense.
-constexpr uint32_t kDenseBit = 0x40000000u;
-
-__device__ __forceinline__ uint32_t own_cell_count(const WalkCtx &W, const WalkStart &s) {
-    const uint32_t k = ((uint32_t)s.mz * (uint32_t)W.grid.gy + (uint32_t)s.my) * (uint32_t)W.grid.gx +
-                       (uint32_t)s.mx;
-    return W.start[k + 1] - W.start[k];
 }
 
 // One lane's scan of chunk slots [lo, hi) of a neighbour row (the chunk
@@ -1189,13 +1173,12 @@ __device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c
 // recorded in that order, are what the force pass and its walkers sum over.
 // Lanes off this path (a bucket collision, or a slot at the grid's x seam,
 // whose three x-adjacent cells are not one run) are listed for
-// k_density_deferred, and particles of cells holding more than kDenseCell
-// for k_density_dense.
+// k_density_deferred.
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
               float4 *__restrict__ fr, NbrList L, RowWarps RW, uint32_t *__restrict__ deferred,
-              uint32_t *__restrict__ dense_list, uint32_t *__restrict__ status) {
+              uint32_t *__restrict__ status) {
     __shared__ PosSmem<kInd> s_chunk[kThreads / 32];
     if (status[0] & kStatusErrorMask) return;
     const uint32_t lane = threadIdx.x & 31u;
@@ -1217,12 +1200,8 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     const float4 pi = G.pos[i];
     WalkStart s;
     walk_start(W, P, pi, s);
-    const bool walkable = valid && s.flags == 0u && s.mx >= 1 && s.mx + 1 < g.gx;
-    // a particle of a crowded cell gets a warp of its own (k_density_dense)
-    const bool dense = walkable && own_cell_count(W, s) > kDenseCell;
-    const bool fast = walkable && !dense;
-    defer_lanes(valid && !walkable, t, deferred, &status[kStatusDeferred]);
-    defer_lanes(dense, t, dense_list, &status[kStatusDenseDensity]);
+    const bool fast = valid && s.flags == 0u && s.mx >= 1 && s.mx + 1 < g.gx;
+    defer_lanes(valid && !fast, t, deferred, &status[kStatusDeferred]);
     if (!__any_sync(0xffffffffu, fast)) return;
     const uint32_t mxlo = __reduce_min_sync(0xffffffffu, fast ? (uint32_t)s.mx : 0xffffffffu);
     const uint32_t mxhi = __reduce_max_sync(0xffffffffu, fast ? (uint32_t)s.mx : 0u);
@@ -1273,151 +1252,6 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
         }
     }
     if (fast) density_finish(P, ks, cnt, lrow != nullptr, i, pi, vel, rp, fr, L);
-}
-
-// ---------------------------------------------------------------- crowded cells
-//
-// Where the fluid clumps (the reference's own physics at the benchmark
-// constants), cells grow to hundreds or thousands of particles and every
-// particle there has as many neighbours.  One lane per particle then walks
-// windows of thousands of candidates, the lanes of a warp diverge on them,
-// and a small scene is a handful of warps on the whole GPU.  So a particle
-// whose own cell holds more than kDenseCell particles gets a warp: its lanes
-// stride over each neighbour row's x window together (coalesced loads, lanes
-// in step), each keeps a compensated partial sum, and a butterfly of
-// compensated (two-sum) additions combines them in a fixed order, the same
-// on every lane.  The criterion is the particle's own cell, not the list
-// length, so the path a particle takes does not depend on the options; its
-// results are deterministic and equal alone and in a batch.
-// First position k in [a, b) of an x-sorted run whose x is >= key (after:
-// > key), else b; every lane of the warp calls it with the same arguments
-// and gets the same answer.  Each round the 32 lanes probe evenly spaced
-// points of [lo, hi) and the range shrinks to the gap after the last probe
-// below the key.
-template <bool kInd>
-__device__ __forceinline__ uint32_t warp_search_x(const WalkCtx &W, uint32_t a, uint32_t b, float key,
-                                                  bool after) {
-    const uint32_t lane = threadIdx.x & 31u;
-    uint32_t lo = a, hi = b;  // the answer lies in [lo, hi]
-    while (hi - lo > 32u) {
-        const uint32_t step = (hi - lo + 31u) >> 5;
-        const uint32_t k = lo + lane * step;
-        bool below = false;
-        if (k < hi) {
-            const float x = W.pos[kInd ? W.order[k] : k].x;
-            below = after ? x <= key : x < key;
-        }
-        const uint32_t c = __popc(__ballot_sync(0xffffffffu, below));
-        if (c == 0u) return lo;  // the first probe, lo itself, is not below
-        const uint32_t nhi = min(lo + c * step, hi);
-        lo += (c - 1u) * step + 1u;
-        hi = nhi;
-    }
-    const uint32_t k = lo + lane;
-    bool below = false;
-    if (k < hi) {
-        const float x = W.pos[kInd ? W.order[k] : k].x;
-        below = after ? x <= key : x < key;
-    }
-    return lo + __popc(__ballot_sync(0xffffffffu, below));
-}
-
-// Compensated sum (s, e: value and error terms) combined across the warp in
-// a fixed butterfly of two-sum additions; every lane returns the total.
-__device__ __forceinline__ float warp_sum_compensated(float s, float e) {
-#pragma unroll
-    for (int d = 16; d; d >>= 1) {
-        const float so = __shfl_xor_sync(0xffffffffu, s, d);
-        const float eo = __shfl_xor_sync(0xffffffffu, e, d);
-        // two-sum: t = s + so exactly as t + err (commutative in s, so)
-        const float t = __fadd_rn(s, so);
-        const float z = __fsub_rn(t, s);
-        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(so, z));
-        s = t;
-        e = __fadd_rn(__fadd_rn(e, eo), err);
-    }
-    return __fadd_rn(s, e);
-}
-
-// The nine neighbour rows of a crowded-cell particle (flags 0, off the x
-// seam) for a whole warp: `row(lo, hi, xlo, xhi)` is called, uniformly across
-// the warp, with the window [lo, hi) of each row's three-cell run the
-// narrowing keeps, in walk order (dz, then dy).  With x-sorted runs the
-// window is cut to [xlo, xhi] by two searches; otherwise it is the whole run
-// and the caller tests x.
-template <bool kInd, class F>
-__device__ __forceinline__ void dense_rows(const WalkCtx &W, const WalkStart &s, float4 pi, F &&row) {
-    const Grid &g = W.grid;
-    const float h = W.h;
-    const float eym = gap_to_cell(pi.y, s.c.cy, -1, h), eyp = gap_to_cell(pi.y, s.c.cy, 1, h);
-    const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
-    const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
-#pragma unroll 1
-    for (int dz = -1; dz <= 1; ++dz) {
-        const float ez2 = dz < 0 ? ezm * ezm : (dz > 0 ? ezp * ezp : 0.f);
-        const uint32_t zrow = (uint32_t)wrap1(s.mz + dz, g.gz) * (uint32_t)g.gy;
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const float ey2 = dy < 0 ? eym * eym : (dy > 0 ? eyp * eyp : 0.f);
-            const float w2 = W.h2w - ey2 - ez2;
-            if (!(w2 > 0.f)) continue;
-            const uint32_t base = (zrow + (uint32_t)wrap1(s.my + dy, g.gy)) * (uint32_t)g.gx;
-            const uint32_t a = W.start[base + s.mx - 1], b = W.start[base + s.mx + 2];
-            if (a == b) continue;
-            const float hx = fmaf(sqrtf(w2), 1.0000009536743164f, xpad);
-            const float xlo = pi.x - hx, xhi = pi.x + hx;
-            uint32_t lo = a, hi = b;
-            if (W.xmono) {
-                lo = warp_search_x<kInd>(W, a, b, xlo, false);
-                hi = warp_search_x<kInd>(W, lo, b, xhi, true);
-            }
-            row(lo, hi, xlo, xhi);
-        }
-    }
-}
-
-// Density of the crowded-cell particles k_density listed, one warp each.
-template <bool kInd>
-__global__ void __launch_bounds__(kDeferredThreads)
-    k_density_dense(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
-                    float4 *__restrict__ fr, NbrList L, const uint32_t *__restrict__ dense_list,
-                    const uint32_t *__restrict__ status) {
-    if (status[0] & kStatusErrorMask) return;
-    const uint32_t m = status[kStatusDenseDensity];
-    const uint32_t lane = threadIdx.x & 31u, nw = gridDim.x * (kDeferredThreads / 32);
-#pragma unroll 1
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < m; q += nw) {
-        const uint32_t t = dense_list[q];
-        const uint32_t i = kInd ? G.order[t] : t;
-        const uint32_t sc = scene_of(T, i);
-        const StepParams &P = T.params[sc];
-        const WalkCtx W = walk_ctx(T, G, sc, P, status);
-        const float4 pi = G.pos[i];
-        WalkStart s;
-        walk_start(W, P, pi, s);
-        float ks = 0.f, kc = 0.f;
-        uint32_t cnt = 0u;
-        const bool xmono = W.xmono;
-        dense_rows<kInd>(W, s, pi, [&](uint32_t lo, uint32_t hi, float xlo, float xhi) {
-#pragma unroll 2
-            for (uint32_t k = lo + lane; k < hi; k += 32u) {
-                const float4 p = G.pos[kInd ? G.order[k] : k];
-                if (!xmono && !(p.x >= xlo && p.x <= xhi)) continue;
-                const float dx = __fsub_rn(p.x, pi.x);
-                const float dy = __fsub_rn(p.y, pi.y);
-                const float dz = __fsub_rn(p.z, pi.z);
-                const float d2 =
-                    __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                if (d2 < W.h2 && k != t) {
-                    kahan_add_cube(ks, kc, __fsub_rn(W.h2, d2));
-                    ++cnt;
-                }
-            }
-        });
-        const float acc = warp_sum_compensated(ks, -kc);
-        cnt = __reduce_add_sync(0xffffffffu, cnt);
-        if (lane == 0) density_finish(P, acc, cnt | kDenseBit, false, i, pi, vel, rp, fr, L);
-    }
 }
 
 // The particles k_density deferred, one warp each (warp_walk).
@@ -1651,17 +1485,13 @@ __global__ void __launch_bounds__(kThreads, kForceListThreadsPerSM / kThreads)
     k_force(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, const float4 *__restrict__ rp,
             const float4 *__restrict__ fr, NbrList L, float4 *__restrict__ pos_out,
             float4 *__restrict__ vel_out, float4 *__restrict__ force_out,
-            uint32_t *__restrict__ walk_warps, uint32_t *__restrict__ dense_list,
-            uint32_t *__restrict__ status) {
+            uint32_t *__restrict__ walk_warps, uint32_t *__restrict__ status) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (status[0] & kStatusErrorMask) return;
     const bool valid = t < T.n;  // the grid is whole blocks: every lane gets here
     const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
     const uint32_t cnt = valid ? L.count[i] : 0u;
-    const bool dense = valid && (cnt & kDenseBit);
-    defer_lanes(dense, t, dense_list, &status[kStatusDenseForce]);
-    const bool walker = valid && !dense && cnt > L.slots;
-    const uint32_t wm = __ballot_sync(0xffffffffu, walker);
+    const uint32_t wm = __ballot_sync(0xffffffffu, valid && cnt > L.slots);
     if (wm && (threadIdx.x & 31u) == (uint32_t)(__ffs(wm) - 1))
         walk_warps[atomicAdd(&status[kStatusWalkWarps], 1u)] = t >> 5;
     if (!valid || cnt > L.slots) return;
@@ -1726,8 +1556,7 @@ __global__ void __launch_bounds__(kThreads, kForceThreadsPerSM / kThreads)
         const uint32_t t = walk_warps[q] * 32u + lane;
         const bool valid = t < T.n;
         const uint32_t i = valid ? (kInd ? G.order[t] : t) : 0u;
-        const uint32_t lc = valid ? L.count[i] : 0u;
-        const bool walker = valid && !(lc & kDenseBit) && lc > L.slots;
+        const bool walker = valid && L.count[i] > L.slots;
         const uint32_t sc = valid ? scene_of(T, i) : 0u;
         const StepParams &P = T.params[sc];
         const float4 pi = G.pos[i];
@@ -1743,57 +1572,6 @@ __global__ void __launch_bounds__(kThreads, kForceThreadsPerSM / kThreads)
         defer_lanes(walker && !cl.fast, t, deferred, &status[kStatusDeferredForce]);
         coop_walk<kInd, true, kTailNone>(W, s, cl, i, pi, scan, v);
         if (cl.fast) force_finish(P, pair, i, pi, vi, r.x, pos_out, vel_out, force_out);
-    }
-}
-
-// Force, integration and walls of the crowded-cell particles k_force
-// listed, one warp each: the lanes stride over each neighbour row's x window
-// of 32-byte neighbour records (k_density_dense's walk), each sums its pairs
-// (ForcePair, compensated), and the three components are combined across the
-// warp in a fixed order.
-template <bool kInd>
-__global__ void __launch_bounds__(kDeferredThreads)
-    k_force_dense(SceneTable T, WalkCtx G, const float4 *__restrict__ vel,
-                  const float4 *__restrict__ rp, const float4 *__restrict__ fr,
-                  float4 *__restrict__ pos_out, float4 *__restrict__ vel_out,
-                  float4 *__restrict__ force_out, const uint32_t *__restrict__ dense_list,
-                  const uint32_t *__restrict__ status) {
-    if (status[0] & kStatusErrorMask) return;
-    const uint32_t m = status[kStatusDenseForce];
-    const uint32_t lane = threadIdx.x & 31u, nw = gridDim.x * (kDeferredThreads / 32);
-#pragma unroll 1
-    for (uint32_t q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < m; q += nw) {
-        const uint32_t t = dense_list[q];
-        const uint32_t i = kInd ? G.order[t] : t;
-        const uint32_t sc = scene_of(T, i);
-        const StepParams &P = T.params[sc];
-        const WalkCtx W = walk_ctx(T, G, sc, P, status);
-        const float4 pi = G.pos[i];
-        const float4 vi = vel[i];
-        const float4 r = rp[i];
-        ForcePair pair{vi, r.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        WalkStart s;
-        walk_start(W, P, pi, s);
-        const bool xmono = W.xmono;
-        dense_rows<kInd>(W, s, pi, [&](uint32_t lo, uint32_t hi, float xlo, float xhi) {
-#pragma unroll 1
-            for (uint32_t k = lo + lane; k < hi; k += 32u) {
-                float4 a, b;
-                load_record(fr, kInd ? G.order[k] : k, a, b);
-                if (!xmono && !(a.x >= xlo && a.x <= xhi)) continue;
-                const float dx = __fsub_rn(a.x, pi.x);
-                const float dy = __fsub_rn(a.y, pi.y);
-                const float dz = __fsub_rn(a.z, pi.z);
-                const float d2 =
-                    __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-                if (d2 < W.h2 && k != t) pair.add(dx, dy, dz, d2, a.w, b);
-            }
-        });
-        ForcePair tot = pair;
-        tot.fx = warp_sum_compensated(pair.fx, -pair.cx);
-        tot.fy = warp_sum_compensated(pair.fy, -pair.cy);
-        tot.fz = warp_sum_compensated(pair.fz, -pair.cz);
-        if (lane == 0) force_finish(P, tot, i, pi, vi, r.x, pos_out, vel_out, force_out);
     }
 }
 
@@ -2154,20 +1932,14 @@ static void density_launch(const SceneTable &T, const WalkCtx &G, const float4 *
                            float4 *fr, const NbrList &L, const RowWarps &RW, bool indirect,
                            uint32_t *deferred, uint32_t *status, cudaStream_t st) {
     const uint32_t threads = launch_threads(T);
-    uint32_t *dense = deferred + dense_density_offset(T.n);
-    const unsigned dense_blocks = std::min<unsigned>(blocks(T.n, kDeferredThreads / 32), kDenseBlocks);
     if (indirect) {
         k_density<true, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(
-            T, G, vel, rp, fr, L, RW, deferred, dense, status);
-        k_density_dense<true><<<dense_blocks, kDeferredThreads, 0, st>>>(T, G, vel, rp, fr, L, dense,
-                                                                        status);
+            T, G, vel, rp, fr, L, RW, deferred, status);
         k_density_deferred<true><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(T, G, vel, rp, fr, L,
                                                                              deferred, status);
     } else {
         k_density<false, kThreads><<<blocks(threads, kThreads), kThreads, 0, st>>>(
-            T, G, vel, rp, fr, L, RW, deferred, dense, status);
-        k_density_dense<false><<<dense_blocks, kDeferredThreads, 0, st>>>(T, G, vel, rp, fr, L, dense,
-                                                                         status);
+            T, G, vel, rp, fr, L, RW, deferred, status);
         k_density_deferred<false><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(T, G, vel, rp, fr, L,
                                                                               deferred, status);
     }
@@ -2183,34 +1955,38 @@ cudaError_t launch_density(const SceneTable &T, const SortBuffers &B, const floa
         const uint32_t ntiles = (T.rows + 1 + kScanTile - 1) / kScanTile;
         k_row_warps<<<ntiles, kScanThreads, 0, st>>>(T, B.start, RW.wofs, B.tile_sum, B.status);
         if (ntiles > 1) k_row_offsets<<<ntiles, kScanThreads, 0, st>>>(T.rows, RW.wofs, B.tile_sum);
-        // both deferred counts, the walker warps' count and their next one,
-        // both crowded-cell counts
-        cudaMemsetAsync(B.status + kStatusDeferred, 0, 24, st);
+        // both deferred counts, the walker warps' count and their next one
+        cudaMemsetAsync(B.status + kStatusDeferred, 0, 16, st);
         if (threads == 128) density_launch<128>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
         else density_launch<256>(T, G, vel, rp, fr, L, RW, indirect, B.deferred, B.status, st);
     }
     return cudaGetLastError();
 }
 
-template <bool kInd, int kThreads>
+template <int kThreads>
 static void force_launch(const SceneTable &T, const WalkCtx &G, const float4 *vel,
                          const float4 *rp, const float4 *fr, const NbrList &L, float4 *pos_out,
-                         float4 *vel_out, float4 *force_out, uint32_t *base, uint32_t *status,
+                         float4 *vel_out, float4 *force_out, bool indirect,
+                         uint32_t *deferred, uint32_t *walk_warps, uint32_t *status,
                          cudaStream_t st) {
-    uint32_t *deferred = base + T.n, *walk_warps = base + 2 * (size_t)T.n;
-    uint32_t *dense = base + dense_force_offset(T.n);
     // the walkers' kernel: as many warps as the GPU holds at once (or fewer)
     const unsigned walk_blocks =
         std::min<unsigned>(blocks(T.n, kThreads), 152u * (kForceThreadsPerSM / kThreads));
-    const unsigned dense_blocks = std::min<unsigned>(blocks(T.n, kDeferredThreads / 32), kDenseBlocks);
-    k_force<kInd, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
-        T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, dense, status);
-    k_force_walk<kInd, kThreads><<<walk_blocks, kThreads, 0, st>>>(
-        T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, deferred, status);
-    k_force_dense<kInd><<<dense_blocks, kDeferredThreads, 0, st>>>(T, G, vel, rp, fr, pos_out, vel_out,
-                                                                  force_out, dense, status);
-    k_force_deferred<kInd><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
-        T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    if (indirect) {
+        k_force<true, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);
+        k_force_walk<true, kThreads><<<walk_blocks, kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, deferred, status);
+        k_force_deferred<true><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    } else {
+        k_force<false, kThreads><<<blocks(T.n, kThreads), kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, status);
+        k_force_walk<false, kThreads><<<walk_blocks, kThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, walk_warps, deferred, status);
+        k_force_deferred<false><<<kDeferredBlocks, kDeferredThreads, 0, st>>>(
+            T, G, vel, rp, fr, L, pos_out, vel_out, force_out, deferred, status);
+    }
 }
 
 cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4 *pos,
@@ -2219,21 +1995,12 @@ cudaError_t launch_force(const SceneTable &T, const SortBuffers &B, const float4
                          cudaStream_t st, int threads) {
     const WalkCtx G = global_ctx(B, pos);
     if (T.n) {
-        if (indirect) {
-            if (threads == 128)
-                force_launch<true, 128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, B.deferred,
-                                        B.status, st);
-            else
-                force_launch<true, 256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, B.deferred,
-                                        B.status, st);
-        } else {
-            if (threads == 128)
-                force_launch<false, 128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, B.deferred,
-                                         B.status, st);
-            else
-                force_launch<false, 256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, B.deferred,
-                                         B.status, st);
-        }
+        if (threads == 128)
+            force_launch<128>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
+                              B.deferred + T.n, B.deferred + 2 * (size_t)T.n, B.status, st);
+        else
+            force_launch<256>(T, G, vel, rp, fr, L, pos_out, vel_out, force_out, indirect,
+                              B.deferred + T.n, B.deferred + 2 * (size_t)T.n, B.status, st);
     }
     return cudaGetLastError();
 }

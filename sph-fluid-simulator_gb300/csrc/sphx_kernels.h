@@ -23,11 +23,9 @@ struct SortBuffers {
     uint32_t *status;    // 2 words: error bits, x-wrap flag (see below)
     uint2 *large;        // cells longer than 64 queued for the block sort
     const uint8_t *cflags;  // slots: collision flags of each slot's own cell, or NULL
-    uint32_t *deferred;  // deferred_entries(n): cell-sorted positions of the particles the
+    uint32_t *deferred;  // 2n + n / 32 + 1: cell-sorted positions of the particles the
                          // density pass (first n) and the force pass (next n) defer,
-                         // the warps of the force pass that hold a walker (n / 32 + 1),
-                         // then the crowded-cell particles of the density pass (n)
-                         // and of the force pass (n)
+                         // then the warps of the force pass that hold a walker
     uint32_t large_cap;  // entries of `large` (n / 64 + 2 suffices)
     uint32_t slots;      // gx * gy * gz
     uint32_t max_cell;   // occupancy above which a step refuses to walk (<= kLargeCell)
@@ -36,11 +34,6 @@ struct SortBuffers {
 // Largest cell the step sorts (shared-memory bitonic sort of 8-byte keys) and
 // the CTAs that share the queued large cells.
 constexpr uint32_t kLargeCell = 16384;
-// Entries of SortBuffers::deferred for n particles, and the offsets of its
-// crowded-cell lists.
-constexpr size_t deferred_entries(size_t n) { return 4 * n + n / 32 + 1; }
-constexpr size_t dense_density_offset(size_t n) { return 2 * n + n / 32 + 1; }
-constexpr size_t dense_force_offset(size_t n) { return 3 * n + n / 32 + 1; }
 constexpr unsigned kLargeBlocks = 152;
 inline uint32_t large_list_cap(uint32_t n) { return n / 64 + 2; }
 
@@ -59,10 +52,6 @@ constexpr uint32_t kStatusDeferred = 4u;
 constexpr uint32_t kStatusDeferredForce = 5u;
 constexpr uint32_t kStatusWalkWarps = 6u;
 constexpr uint32_t kStatusWalkNext = 7u;
-// status[8], status[9]: particles of crowded cells the density and force
-// passes hand to their warp-per-particle kernels (cleared with the above).
-constexpr uint32_t kStatusDenseDensity = 8u;
-constexpr uint32_t kStatusDenseForce = 9u;
 
 cudaError_t launch_sort(const SceneTable &T, const SortBuffers &B, const float4 *pos,
                         cudaStream_t st);

@@ -17,7 +17,7 @@
 // Limits and sharing:
 //   * at most kMaxParticles (131,072) particles per call; more is rejected
 //     with SPHX_ERR_INVALID;
-//   * the array (about 8.6 MiB) lives in every GPU that loads the library
+//   * the array (about 7 MiB) lives in every GPU that loads the library
 //     until the process exits;
 //   * every call on a device uses the same array, which keeps the previous
 //     call's contents: the counts and status words are cleared at the start
@@ -63,7 +63,7 @@ constexpr size_t kOffLarge = kOffRp + 16ull * kMaxParticles;  // queued large ce
 constexpr size_t kOffScat = kOffLarge + align256(8ull * (kMaxParticles / 64 + 2));
 constexpr size_t kOffDeferred = kOffScat + 8ull * kMaxParticles;
 constexpr uint32_t kRows = (uint32_t)kGridDim * kGridDim;  // cell rows of the grid
-constexpr size_t kOffRowWarps = kOffDeferred + align256(4ull * sphx::deferred_entries(kMaxParticles));
+constexpr size_t kOffRowWarps = kOffDeferred + align256(4ull * kMaxParticles);
 constexpr size_t kScratchBytes = kOffRowWarps + align256(4ull * (kRows + 1));
 static_assert(sizeof(sphx::StepParams) + 24 <= 1024, "scene table fits its scratch slot");
 
