@@ -293,7 +293,9 @@ def serve_sweep(sphx, count, rates, tick, device):
         results.append({"rate_per_s": lam, "span_s": span,
                         "served": {"scenes_per_s": len(reqs) / span, "p50_s": q(lat, 50),
                                    "p95_s": q(lat, 95), "p99_s": q(lat, 99),
-                                   "relayouts": int(st.relayouts), "ticks": int(st.ticks)},
+                                   "relayouts": int(st.relayouts), "ticks": int(st.ticks),
+                                   "worker_s": {"layout": st.layout_s, "step": st.step_s,
+                                                "readout": st.readout_s}},
                         "sequential": {"scenes_per_s": len(reqs) / span_seq, "p50_s": q(lat_seq, 50),
                                        "p95_s": q(lat_seq, 95), "p99_s": q(lat_seq, 99)},
                         "speedup": span_seq / span})

@@ -303,6 +303,10 @@ typedef struct sphx_server_stats {
     uint64_t submitted, completed, ticks, relayouts, particle_steps;
     size_t live_scenes, queued, bytes_in_use;
     double elapsed_s;
+    /* worker time laying scenes out (admission, retirement), stepping (to
+     * the end of each tick's steps on the device) and copying finished
+     * scenes' results back */
+    double layout_s, step_s, readout_s;
 } sphx_server_stats;
 
 void sphx_server_options_default(sphx_server_options *o);

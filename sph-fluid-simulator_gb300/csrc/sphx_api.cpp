@@ -274,7 +274,7 @@ int upload_scene(sphx_handle *h, const sphx::Scene &sc, const float *pos3, const
     if (vel3) SPHX_CUDA(cudaMemcpyAsync(sv, vel3, 12 * n, cudaMemcpyHostToDevice, h->stream));
     else SPHX_CUDA(cudaMemsetAsync(sv, 0, 12 * n, h->stream));
     SPHX_CUDA(sphx::launch_upload_rows(sc.first, sc.n, sp, sv, h->pos[pv], h->vel[pv], h->id[idc],
-                                       sc.d.h, bad, keep_order, h->stream));
+                                       sc.d.h, bad, keep_order, h->sb.status, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));  // staging is reused by the next scene
     return SPHX_OK;
 }
@@ -806,10 +806,9 @@ int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3) {
     // step's cell order, which the next step's sort then finds sorted; but
     // only while every step so far completed: a step that stopped on an
     // error did not move the ids with the data, and the state is then
-    // rewritten in id order instead.
-    SPHX_CUDA(cudaMemcpyAsync(h->h_status, h->sb.status, 4, cudaMemcpyDeviceToHost, h->stream));
-    SPHX_CUDA(cudaStreamSynchronize(h->stream));
-    const bool keep = h->error == 0 && (*h->h_status & sphx::kStatusErrorMask) == 0;
+    // rewritten in id order instead (the upload kernel checks the device's
+    // error bits itself).
+    const bool keep = h->error == 0;
     SPHX_CUDA(cudaMemsetAsync(bad, 0xFF, 4, h->stream));
     for (const sphx::Scene &sc : h->scenes) {
         const int rc = upload_scene(h, sc, pos3 + 3ull * sc.first,

@@ -1661,15 +1661,19 @@ __global__ void k_digest(SceneTable T, WalkCtx G, const uint32_t *__restrict__ i
 // id becomes i (scene-local).  With keep_order, every row keeps its particle
 // (id[row]) and takes that particle's values: the storage stays in the cell
 // order of the last step, so the next step's sort and gather find it sorted.
+// keep_order holds only while no step stopped on an error since the last
+// upload (status word 0 clear): such a step leaves the ids behind the data.
 // With `bad` set, a position that is non-finite or whose cell quotient x / h
 // is 2^30 or more in magnitude (the host check of a new scene, done here for
 // state replacements) lowers *bad to first + its particle index.
 __global__ void k_upload_rows(uint32_t first, uint32_t n, const float *__restrict__ pos3,
                               const float *__restrict__ vel3, float4 *__restrict__ pos,
                               float4 *__restrict__ vel, uint32_t *__restrict__ id, float h,
-                              uint32_t *__restrict__ bad, bool keep_order) {
+                              uint32_t *__restrict__ bad, bool keep_order,
+                              const uint32_t *__restrict__ status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    keep_order = keep_order && !(status[0] & kStatusErrorMask);
     const uint32_t r = first + i;
     // the particle (index into the staging arrays); an id outside the scene
     // (never, while the ids are a permutation) falls back to the row's index
@@ -2022,10 +2026,10 @@ cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float
 
 cudaError_t launch_upload_rows(uint32_t first, uint32_t n, const float *pos3, const float *vel3,
                                float4 *pos, float4 *vel, uint32_t *id, float h, uint32_t *bad,
-                               bool keep_order, cudaStream_t st) {
+                               bool keep_order, const uint32_t *status, cudaStream_t st) {
     if (n)
         k_upload_rows<<<blocks(n, 256), 256, 0, st>>>(first, n, pos3, vel3, pos, vel, id, h, bad,
-                                                      keep_order);
+                                                      keep_order && status, status);
     return cudaGetLastError();
 }
 

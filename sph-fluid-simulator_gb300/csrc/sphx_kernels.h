@@ -103,10 +103,11 @@ cudaError_t launch_digest(const SceneTable &T, const SortBuffers &B, const float
 // 2 force, 3 rho, 4 prs).
 // bad: NULL, or a device word lowered to first + the index of the first
 // particle whose position is outside the walk's domain for cell size h.
-// keep_order: rows keep their particles (id unchanged), see k_upload_rows.
+// keep_order: rows keep their particles (id unchanged) unless the sticky
+// error bits of status (word 0) are set, see k_upload_rows.
 cudaError_t launch_upload_rows(uint32_t first, uint32_t n, const float *pos3, const float *vel3,
                                float4 *pos, float4 *vel, uint32_t *id, float h, uint32_t *bad,
-                               bool keep_order, cudaStream_t st);
+                               bool keep_order, const uint32_t *status, cudaStream_t st);
 // Dam-break lattice generated on the device into rows [first, first + n).
 struct LatticeGen {
     uint32_t nx, ny, nz;

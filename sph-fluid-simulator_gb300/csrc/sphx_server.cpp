@@ -100,6 +100,16 @@ void sphx_server::run() {
         }
         lock.unlock();
         int rc = SPHX_OK;
+        // where the tick's time goes: laying scenes out, stepping, reading
+        // finished scenes back (added to the stats under the lock below)
+        double t_layout = 0, t_step = 0, t_read = 0;
+        uint64_t n_layouts = 0, n_steps = 0;
+        auto t = Clock::now();
+        auto lap = [&](double &acc) {
+            const auto now = Clock::now();
+            acc += std::chrono::duration<double>(now - t).count();
+            t = now;
+        };
         if (!admitted.empty()) {
             std::vector<sphx::SceneInit> inits;
             for (size_t k = 0; k < live.size(); ++k) {
@@ -126,7 +136,8 @@ void sphx_server::run() {
                 rc = sphx::relayout(h, inits);
             }
             for (Request *r : admitted) live.push_back(r);
-            stats.relayouts += 1;
+            n_layouts += 1;
+            lap(t_layout);
         }
         // One tick: every live scene advances by the same number of steps.
         int k = opt.steps_per_tick;
@@ -140,10 +151,10 @@ void sphx_server::run() {
         }
         if (rc == SPHX_OK && k > 0) rc = sphx::run_steps(h, opt.dt, k);
         if (rc == SPHX_OK) rc = sphx::read_status(h);
+        lap(t_step);
         std::vector<int> finished;
         if (rc == SPHX_OK) {
-            stats.ticks += 1;
-            stats.particle_steps += (uint64_t)h->n * (uint64_t)k;
+            n_steps = (uint64_t)h->n * (uint64_t)k;
             for (size_t j = 0; j < live.size(); ++j) {
                 Request *r = live[j];
                 r->steps_done += k;
@@ -159,6 +170,7 @@ void sphx_server::run() {
                 }
             }
         }
+        lap(t_read);
         if (rc == SPHX_OK && !finished.empty()) {
             std::vector<sphx::SceneInit> inits;
             size_t f = 0;
@@ -172,8 +184,18 @@ void sphx_server::run() {
                 inits.push_back(in);
             }
             rc = sphx::relayout(h, inits);
+            n_layouts += 1;
+            lap(t_layout);
         }
         lock.lock();
+        stats.relayouts += n_layouts;
+        stats.layout_s += t_layout;
+        stats.step_s += t_step;
+        stats.readout_s += t_read;
+        if (rc == SPHX_OK) {
+            stats.ticks += 1;
+            stats.particle_steps += n_steps;
+        }
         if (rc != SPHX_OK) {
             fatal = rc;
             fatal_msg = sphx_last_error();
@@ -197,13 +219,13 @@ void sphx_server::run() {
         if (!finished.empty()) {
             std::vector<Request *> keep;
             size_t f = 0;
-            const double t = now();
+            const double t_done = now();
             for (size_t j = 0; j < live.size(); ++j) {
                 if (f < finished.size() && finished[f] == (int)j) {
                     ++f;
                     Request *r = live[j];
                     r->state = SPHX_REQ_DONE;
-                    r->done_s = t;
+                    r->done_s = t_done;
                     bytes_in_use -= r->bytes;
                     stats.completed += 1;
                 } else {

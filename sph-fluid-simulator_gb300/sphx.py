@@ -107,7 +107,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("ticks", C.c_uint64),
                 ("relayouts", C.c_uint64), ("particle_steps", C.c_uint64),
                 ("live_scenes", C.c_size_t), ("queued", C.c_size_t),
-                ("bytes_in_use", C.c_size_t), ("elapsed_s", C.c_double)]
+                ("bytes_in_use", C.c_size_t), ("elapsed_s", C.c_double),
+                ("layout_s", C.c_double), ("step_s", C.c_double), ("readout_s", C.c_double)]
 
 
 _lib = None
