@@ -304,6 +304,9 @@ def serve_sweep(sphx, count, rates, tick, device):
             "hbm_budget_gb": 150, "rates": results,
             # no schedule can finish the stream before its longest request
             # finishes alone: the served span's floor
+            "requests_n": [int(len(p)) for _, p, _, _ in reqs],
+            "requests_steps": [int(k) for _, _, _, k in reqs],
+            "service_s": [round(float(x), 4) for x in service],
             "longest_request_alone_s": float(max(service)),
             "sequential_total_s": float(sum(service)),
             "speedup_bound": float(sum(service)) / float(max(service)),
@@ -466,6 +469,7 @@ def run_sphx(a):
     # warm-up, then the timed region with per-phase events recorded inside it
     sc.step(sphx.DT, a.warmup)
     sc.synchronize()
+    st0 = sc.read()  # the window's first state: the e2e leg below starts from it
     walk0 = sc.walk_stats()  # (r^2 tests, accepted pairs) of the window's first step
     sc.set_profiling(True)
     sc.kernel_times()  # reset accumulators
@@ -513,26 +517,30 @@ def run_sphx(a):
 
     # e2e through the C-ABI with pinned host buffers: every step uploads the
     # state, steps (graph replay, as a user's handle does) and reads
-    # positions and velocities back.  The state is the window's last one.
+    # positions and velocities back, from the timed window's first state.
     pin_pos = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
     pin_vel = torch.empty((n, 3), dtype=torch.float32, pin_memory=True).numpy()
-    st = sc.read()
-    pin_pos[:] = st["pos"]
-    pin_vel[:] = st["vel"]
+    pin_pos[:] = st0["pos"]
+    pin_vel[:] = st0["vel"]
     sc.close()
     sc = sphx.Scene(s, box, pin_pos, pin_vel,
                     sphx.default_options(device=device, reorder_interval=a.reorder, use_graph=1))
     e2e_steps = max(1, min(a.steps, 10))
     lib = sphx.lib()
 
+    e2e_stream = torch.cuda.ExternalStream(sc.device_view().stream, device=device)
+
     def e2e_iteration():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
         t0 = time.perf_counter()
         sc.set_state(pin_pos, pin_vel)
         t1 = time.perf_counter()
+        ev[0].record(e2e_stream)
         sc.step(sphx.DT, 1)
+        ev[1].record(e2e_stream)
         sphx._check(lib.sphx_read_state(sc.h, sphx._ptr(pin_pos), sphx._ptr(pin_vel), None, None,
                                         None))
-        return t1 - t0, time.perf_counter() - t1
+        return t1 - t0, time.perf_counter() - t1, ev[0].elapsed_time(ev[1])
 
     for _ in range(3):
         e2e_iteration()
@@ -544,17 +552,18 @@ def run_sphx(a):
     t_e2e = max_over_ranks(t_e2e)
     sc.close()
     ceil = copy_ceiling(torch, 24 * n)
-    step_ms = ms / a.steps
+    step_ms = float(np.mean([p[2] for p in parts]))  # device time of the e2e steps themselves
     copy_ms = 1e3 * 24 * n * (1.0 / ceil["h2d_gbs"] + 1.0 / ceil["d2h_gbs"]) / 1e9
     e2e = {"value": n * e2e_steps * world / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 24 * n,
            "ms_per_step": 1e3 * t_e2e / e2e_steps,
            "upload_ms": 1e3 * float(np.mean([p[0] for p in parts])),
            "step_and_readout_ms": 1e3 * float(np.mean([p[1] for p in parts])),
+           "device_step_ms": step_ms,
            "copy_ceiling": ceil,
            "bound_ms": step_ms + copy_ms,
-           "bound_note": "device step of the timed window + 24 B/particle each way at the measured "
-                         "single-copy pinned rates",
+           "bound_note": "device time of the e2e steps (CUDA events on the handle's stream) + 24 "
+                         "B/particle each way at the measured single-copy pinned rates",
            "path": "sphx_set_state + sphx_step (graph replay) + sphx_read_state (pinned host buffers)"}
 
     # The configured runs (200 steps from the initial lattice): the fluid
