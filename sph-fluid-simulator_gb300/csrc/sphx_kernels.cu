@@ -830,11 +830,34 @@ struct PosScan {
                                          float4 pi) {
         test_pair(W, kInd ? sm.idx[k] : c0 + k, sm.p(k), self, pi, 1u, vis);
     }
-    // Every candidate of chunk slots [lo, hi), with weight w (scan_run's test).
-    __device__ __forceinline__ void test_all(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
-                                             uint32_t self, float4 pi, uint32_t w) {
-        for (uint32_t k = lo; k < hi; ++k)
-            test_pair(W, kInd ? sm.idx[k] : c0 + k, sm.p(k), self, pi, w, vis);
+    // Every candidate of chunk slots [0, m), with weight w, for a whole warp
+    // walking one particle: lane l tests slot l (the reference's float r^2),
+    // then lane 0 hands the accepted ones to its visitor in slot order, w
+    // times each: scan_run's visits, in its order, with its values.
+    __device__ __forceinline__ void test_all_warp(const WalkCtx &W, uint32_t c0, uint32_t m,
+                                                  uint32_t self, float4 pi, uint32_t w) {
+        const uint32_t lane = threadIdx.x & 31u;
+        bool acc = false;
+        float d2 = 0.f;
+        uint32_t j = 0u;
+        if (lane < m) {
+            const float4 p = sm.p(lane);
+            j = kInd ? sm.idx[lane] : c0 + lane;
+            const float dx = __fsub_rn(p.x, pi.x);
+            const float dy = __fsub_rn(p.y, pi.y);
+            const float dz = __fsub_rn(p.z, pi.z);
+            d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            acc = d2 < W.h2 && j != self;
+        }
+        uint32_t mask = __ballot_sync(0xffffffffu, acc);
+        while (mask) {  // warp-uniform
+            const int l = __ffs(mask) - 1;
+            mask &= mask - 1u;
+            const float dl = __shfl_sync(0xffffffffu, d2, l);
+            const uint32_t jl = __shfl_sync(0xffffffffu, j, l);
+            if (lane == 0)
+                for (uint32_t r = 0; r < w; ++r) vis(jl, 0.f, 0.f, 0.f, dl);
+        }
     }
     // Chunk slots [lo, hi), the chunk starting at cell-sorted slot c0; true
     // once past the window's end.
@@ -870,11 +893,12 @@ struct PosScan {
 
 // One particle's walk by a whole warp, for the particles the walk kernels
 // defer.  The lanes copy each cell's run into the scanner's chunk, 32
-// candidates at a time, and lane 0 tests them in order: the same cells, order
-// and weights as walk() (the slow path's cells where buckets collide, else
-// the 27 cells row by row, which is walk_rows' order), so the sums are
-// walk()'s bit for bit, while the loads of a candidate run go out together
-// instead of one dependent load after another.
+// candidates at a time, test one candidate each, and lane 0 visits the
+// accepted ones in order: the same cells, order and weights as walk() (the
+// slow path's cells where buckets collide, else the 27 cells row by row,
+// which is walk_rows' order), so the sums are walk()'s bit for bit, while
+// the loads and the r^2 tests of a candidate run go out together instead of
+// one after another.
 template <bool kInd, class S>
 __device__ __forceinline__ void warp_walk_cell(const WalkCtx &W, uint32_t k, uint32_t w,
                                                uint32_t self, float4 pi, S &scan) {
@@ -885,7 +909,7 @@ __device__ __forceinline__ void warp_walk_cell(const WalkCtx &W, uint32_t k, uin
         const uint32_t m = min(32u, b - c0);
         if (lane < m) scan.load(W, lane, kInd ? W.order[c0 + lane] : c0 + lane);
         __syncwarp();
-        if (lane == 0) scan.test_all(W, c0, 0u, m, self, pi, w);
+        scan.test_all_warp(W, c0, m, self, pi, w);
         __syncwarp();
     }
 }
@@ -1363,20 +1387,30 @@ struct RecordScan {
         sm.b[k] = fr[2 * (size_t)j + 1];
         if (kInd) sm.idx[k] = j;
     }
-    // Every candidate of chunk slots [lo, hi), with weight w: the pairs of
-    // ForceVisitor under scan_run, from the chunk's records.
-    __device__ __forceinline__ void test_all(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
-                                             uint32_t self, float4 pi, uint32_t w) {
-        for (uint32_t k = lo; k < hi; ++k) {
-            const float4 p = sm.a[k];
+    // Every candidate of chunk slots [0, m), with weight w, for a whole warp
+    // walking one particle: lane l tests slot l, then lane 0 adds the
+    // accepted pairs from the chunk's records in slot order, w times each:
+    // ForceVisitor's pairs under scan_run, in its order.
+    __device__ __forceinline__ void test_all_warp(const WalkCtx &W, uint32_t c0, uint32_t m,
+                                                  uint32_t self, float4 pi, uint32_t w) {
+        const uint32_t lane = threadIdx.x & 31u;
+        bool acc = false;
+        if (lane < m) {
+            const float4 p = sm.a[lane];
             const float dx = __fsub_rn(p.x, pi.x);
             const float dy = __fsub_rn(p.y, pi.y);
             const float dz = __fsub_rn(p.z, pi.z);
             const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            const uint32_t j = kInd ? sm.idx[k] : c0 + k;
-            if (d2 < W.h2 && j != self)
-                for (uint32_t r = 0; r < w; ++r) pair_add_record(pair, p, sm.b[k], pi);
+            const uint32_t j = kInd ? sm.idx[lane] : c0 + lane;
+            acc = d2 < W.h2 && j != self;
         }
+        uint32_t mask = __ballot_sync(0xffffffffu, acc);
+        if (lane == 0)
+            while (mask) {
+                const uint32_t k = __ffs(mask) - 1;
+                mask &= mask - 1u;
+                for (uint32_t r = 0; r < w; ++r) pair_add_record(pair, sm.a[k], sm.b[k], pi);
+            }
     }
     __device__ __forceinline__ bool scan(const WalkCtx &W, uint32_t c0, uint32_t lo, uint32_t hi,
                                          float xlo, float xhi, uint32_t self, float4 pi) {
