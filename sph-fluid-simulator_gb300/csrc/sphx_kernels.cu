@@ -1327,9 +1327,17 @@ struct ForcePair {
         const float hd = h - r;
         const float cp = kp * (presI + pj_w) * vj.w * (hd * hd) * invr;
         const float cv = kv * hd * vj.w;
-        kahan_add(fx, cx, fmaf(cv, vj.x - vi.x, -cp * dx));
-        kahan_add(fy, cy, fmaf(cv, vj.y - vi.y, -cp * dy));
-        kahan_add(fz, cz, fmaf(cv, vj.z - vi.z, -cp * dz));
+        // compensated add of cv (vj - vi) - cp d: the term minus the running
+        // compensation in two fused multiply-adds (one rounding each)
+        kahan_add_term(fx, cx, fmaf(cv, vj.x - vi.x, fmaf(-cp, dx, -cx)));
+        kahan_add_term(fy, cy, fmaf(cv, vj.y - vi.y, fmaf(-cp, dy, -cy)));
+        kahan_add_term(fz, cz, fmaf(cv, vj.z - vi.z, fmaf(-cp, dz, -cz)));
+    }
+    // The rest of kahan_add given y = term - c.
+    __device__ __forceinline__ static void kahan_add_term(float &s, float &c, float y) {
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
     }
 };
 
