@@ -1092,7 +1092,11 @@ __device__ __forceinline__ WalkCtx walk_ctx(const SceneTable &T, const WalkCtx &
 // Threads and blocks of the kernels that take the deferred particles: few
 // in fluid (none in the dam-break block), at most n.
 constexpr int kDeferredThreads = 128;
-constexpr unsigned kDeferredBlocks = 2 * 152;
+// Eight blocks per SM: a batch of small scenes near the origin (where
+// buckets collide) defers thousands of particles, and a deferred walk is a
+// chain of dependent loads that wants other warps beside it (the 512-scene
+// step took 3.43 ms against 3.54 with two blocks per SM).
+constexpr unsigned kDeferredBlocks = 8 * 152;
 // No list is recorded for a particle whose cell holds more than
 // slots / kListSkipFactor particles; its count then carries kNoList.
 constexpr uint32_t kListSkipFactor = 4;
