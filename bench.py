@@ -34,11 +34,12 @@ UNIT = "particle-steps/s"
 SIDE = 128  # 128^3 = 2,097,152 particles
 ALGO_BYTES = 80  # density 24 B + force 56 B per particle-step (compulsory FP32 SoA)
 # FP32 operations of the walk kernels: an r^2 test is 3 sub + 3 mul + 2 add;
-# an accepted pair costs the density 1 sub + 2 mul (cube) + 4 (compensated
-# add) and the force 41 (distance 8, rsqrt, r and h - r 2, two coefficients
-# 6, three components 3 x 4, compensated adds 12)
+# an accepted pair costs the density 1 sub + 1 mul + 1 fused multiply-add
+# (the cube added to its row's sum) and the force 41 (distance 8, rsqrt, r
+# and h - r 2, two coefficients 6, three components 3 x 4, compensated adds
+# 12)
 OPS_PER_TEST = 8
-OPS_PER_PAIR_DENSITY = 7
+OPS_PER_PAIR_DENSITY = 4
 OPS_PER_PAIR_FORCE = 41
 WORKLOAD = ("dam-break block 128^3 = 2,097,152 particles, jittered cubic lattice spacing 0.05 m "
             "(+-5%), box 16 x 8 x 8 m (walls at bound +- h, floor y=0, no ceiling), h=0.1, "

@@ -435,11 +435,30 @@ __device__ __forceinline__ int wrap1(int v, int m) {
     return v >= m ? v - m : v;
 }
 
+// The nine (dy, dz) neighbour rows of a cell, in the order every walk
+// visits them: the dz = 0 layer, then dz = +1, then dz = -1, each as
+// dy = -1, 0, +1.  (k_density takes the first three as one group and the
+// last six as another: the z layers on either side of a particle hold
+// complementary x windows, so a lane's work over the pair varies little.)
+__device__ __forceinline__ int row_dz(int r) { return r < 3 ? 0 : (r < 6 ? 1 : -1); }
+__device__ __forceinline__ int row_dy(int r) { return r % 3 - 1; }
+
 // Fast path: the 27 cells around (mx, my, mz), each visited once.
 __device__ __forceinline__ uint32_t row_base(const Grid &g, int my, int mz, int r) {
-    const int z = wrap1(mz + r / 3 - 1, g.gz);
-    const int y = wrap1(my + r % 3 - 1, g.gy);
+    const int z = wrap1(mz + row_dz(r), g.gz);
+    const int y = wrap1(my + row_dy(r), g.gy);
     return ((uint32_t)z * (uint32_t)g.gy + (uint32_t)y) * (uint32_t)g.gx;
+}
+
+// Squared half-width budget of row r's x window: h^2 (widened) less the
+// squared gaps to the row in y and z (ey2m, ey2p, ez2m, ez2p: below and
+// above); the row holds no accepted neighbour unless it is positive.
+__device__ __forceinline__ float row_w2(float h2w, float ey2m, float ey2p, float ez2m, float ez2p,
+                                        int r) {
+    const int dy = row_dy(r), dz = row_dz(r);
+    const float ey = dy < 0 ? ey2m : (dy > 0 ? ey2p : 0.f);
+    const float ez = dz < 0 ? ez2m : (dz > 0 ? ez2p : 0.f);
+    return h2w - ey - ez;
 }
 
 // Lower bound on the distance from coordinate y (quotient cell c) to any
@@ -482,7 +501,7 @@ __device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, in
         uint32_t rows = 0;
 #pragma unroll
         for (int r = 0; r < 9; ++r)
-            if (W.h2w - ey2[r % 3] - ez2[r / 3] > 0.f) rows |= 1u << r;
+            if (W.h2w - ey2[r % 3] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
         const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
         int r = __ffs(rows) - 1;
         rows &= rows - 1;
@@ -499,7 +518,7 @@ __device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, in
                 a = W.start[base + mx - 1];
                 b = W.start[base + mx + 2];
             }
-            const int iy = cr % 3, iz = cr / 3;
+            const int iy = cr % 3, iz = row_dz(cr) + 1;
             const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
             const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
             const float hx = fmaf(sqrtf(W.h2w - eyy - ezz), 1.0000009536743164f, xpad);
@@ -668,7 +687,7 @@ __device__ __forceinline__ void coop_rows_group(const WalkCtx &W, const WalkStar
     uint32_t rows = 0;
 #pragma unroll
     for (int r = 0; r < 9; ++r)
-        if (W.h2w - ey2[r % 3] - ez2[r / 3] > 0.f) rows |= 1u << r;
+        if (W.h2w - ey2[r % 3] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
     const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
     uint32_t todo = __reduce_or_sync(gmask, rows);
     const uint32_t mxlo = __reduce_min_sync(gmask, (uint32_t)s.mx);
@@ -681,7 +700,7 @@ __device__ __forceinline__ void coop_rows_group(const WalkCtx &W, const WalkStar
         const uint32_t base = row_base(W.grid, s.my, s.mz, r);
         const uint32_t A = W.start[base + mxlo - 1], B = W.start[base + mxhi + 2];
         const uint32_t a = W.start[base + s.mx - 1], b = W.start[base + s.mx + 2];
-        const int iy = r % 3, iz = r / 3;
+        const int iy = r % 3, iz = row_dz(r) + 1;
         const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
         const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
         bool done = !((rows >> r) & 1u) || a == b;
@@ -718,7 +737,7 @@ __device__ __forceinline__ void coop_rows_warp(const WalkCtx &W, const WalkStart
         ez2[2] = ezp * ezp;
 #pragma unroll
         for (int r = 0; r < 9; ++r)
-            if (W.h2w - ey2[r % 3] - ez2[r / 3] > 0.f) rows |= 1u << r;
+            if (W.h2w - ey2[r % 3] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
     }
     const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
     uint32_t todo = __reduce_or_sync(0xffffffffu, rows);
@@ -738,7 +757,7 @@ __device__ __forceinline__ void coop_rows_warp(const WalkCtx &W, const WalkStart
         }
         A = __shfl_sync(0xffffffffu, A, leader);
         B = __shfl_sync(0xffffffffu, B, leader);
-        const int iy = r % 3, iz = r / 3;
+        const int iy = r % 3, iz = row_dz(r) + 1;
         const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
         const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
         bool done = !member || !((rows >> r) & 1u) || a == b;
@@ -1140,23 +1159,23 @@ __device__ __forceinline__ void density_finish(const StepParams &P, float acc, u
 // holds cell-sorted positions c0, c0 + 1, ...): every candidate inside the
 // lane's x window is tested with the reference's float r^2 (sph.cpp:57: (dx*dx
 // + dy*dy) + dz*dz, no fused multiply-add); an accepted one adds
-// (h^2 - r^2)^3 to the compensated sum and its index to the list row (while
-// it has room).  x-sorted runs (xmono): start at the first x >= xlo
-// (binary search), stop at the first x > xhi; returns true once past the
-// window.  Otherwise every slot is checked against the window.
+// (h^2 - r^2)^3 to the row's sum rs (one fused multiply-add) and its index
+// to the list row (while it has room).  x-sorted runs (xmono): start at the
+// first x >= xlo (binary search), stop at the first x > xhi; returns true
+// once past the window.  Otherwise every slot is checked against the window.
 template <bool kInd>
 __device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c0, uint32_t lo,
                                              uint32_t hi, float xlo, float xhi, bool xmono,
-                                             float4 pi, float h2, uint32_t self, float &ks,
-                                             float &kc, uint32_t &cnt, uint32_t *lrow,
-                                             uint32_t lcap) {
+                                             float4 pi, float h2, uint32_t self, float &rs,
+                                             uint32_t &cnt, uint32_t *lrow, uint32_t lcap) {
     auto visit = [&](uint32_t k, float4 p) {
         const float dx = __fsub_rn(p.x, pi.x);
         const float dy = __fsub_rn(p.y, pi.y);
         const float dz = __fsub_rn(p.z, pi.z);
         const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
         if (d2 < h2 && c0 + k != self) {
-            kahan_add_cube(ks, kc, __fsub_rn(h2, d2));
+            const float u = __fsub_rn(h2, d2);
+            rs = __fmaf_rn(__fmul_rn(u, u), u, rs);
             // streaming store: the force pass reads the row once, after
             // every other row has been written
             if (cnt < lcap) __stcs(lrow + cnt, kInd ? sm.idx[k] : c0 + k);
@@ -1187,20 +1206,23 @@ __device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c
 
 // Density and pressure, sph.cpp:28-76, one warp per cell-row segment (the
 // warps k_row_warps counted).  The reference accumulates m*poly6*(h^2-r^2)^3
-// term by term; here the cubes are summed (compensated) and scaled once: the
-// two differ by float rounding only.
+// term by term; here the cubes of each neighbour row are summed with fused
+// multiply-adds, the nine row sums are added with compensation (Kahan) and
+// the total is scaled once: the two differ by float rounding only (a row
+// holds a fifth of the terms; the row sums are what keeps a long sum of
+// clumped fluid accurate).
 //
 // A warp's particles are up to 32 consecutive cell-sorted particles of one
 // row of slots (my, mz), hence x-sorted, and share its nine neighbour rows.
-// Row, scene and grid are warp-uniform.  For each neighbour row (dz, then dy,
-// the order walk_rows visits them) the warp copies the union of its lanes'
-// three-cell runs into its shared-memory chunk (coalesced, kCoopChunk
-// positions at a time) and every lane scans its own x window of its own run
-// there (density_scan); a row the narrowing rules out for every lane is
-// skipped.  The pairs and their order are walk_rows': the neighbour lists,
-// recorded in that order, are what the force pass and its walkers sum over.
-// Lanes off this path (a bucket collision, or a slot at the grid's x seam,
-// whose three x-adjacent cells are not one run) are listed for
+// Row, scene and grid are warp-uniform.  For each neighbour row, in walk
+// order (row_base), the warp copies the union of its lanes' three-cell runs
+// into its shared-memory chunk (coalesced, kCoopChunk positions at a time)
+// and every lane scans its own x window of its own run there
+// (density_scan); a row the narrowing rules out for every lane is skipped.
+// The pairs and their order are walk_rows': the neighbour lists, recorded
+// in that order, are what the force pass and its walkers sum over.  Lanes
+// off this path (a bucket collision, or a slot at the grid's x seam, whose
+// three x-adjacent cells are not one run) are listed for
 // k_density_deferred.
 template <bool kInd, int kThreads>
 __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
@@ -1235,8 +1257,12 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     const uint32_t mxhi = __reduce_max_sync(0xffffffffu, fast ? (uint32_t)s.mx : 0u);
     // narrowing: lower bounds on the distance to the rows above and below
     const float h = P.h;
-    const float eym = gap_to_cell(pi.y, s.c.cy, -1, h), eyp = gap_to_cell(pi.y, s.c.cy, 1, h);
-    const float ezm = gap_to_cell(pi.z, s.c.cz, -1, h), ezp = gap_to_cell(pi.z, s.c.cz, 1, h);
+    float ey2m = gap_to_cell(pi.y, s.c.cy, -1, h), ey2p = gap_to_cell(pi.y, s.c.cy, 1, h);
+    float ez2m = gap_to_cell(pi.z, s.c.cz, -1, h), ez2p = gap_to_cell(pi.z, s.c.cz, 1, h);
+    ey2m *= ey2m;
+    ey2p *= ey2p;
+    ez2m *= ez2m;
+    ez2p *= ez2p;
     const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
     uint32_t *lrow = fast ? density_row(W, s, L, i) : nullptr;
     const uint32_t lcap = lrow ? L.slots : 0u;
@@ -1244,40 +1270,36 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     uint32_t cnt = 0u;
     PosSmem<kInd> &sm = s_chunk[threadIdx.x >> 5];
 #pragma unroll 1
-    for (int dz = -1; dz <= 1; ++dz) {
-        const float ez2 = dz < 0 ? ezm * ezm : (dz > 0 ? ezp * ezp : 0.f);
-        const uint32_t zrow = (uint32_t)wrap1(mz + dz, g.gz) * gy;
-#pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const float ey2 = dy < 0 ? eym * eym : (dy > 0 ? eyp * eyp : 0.f);
-            const float w2 = W.h2w - ey2 - ez2;
-            const bool need = fast && w2 > 0.f;
-            if (!__any_sync(0xffffffffu, need)) continue;
-            const uint32_t base = (zrow + (uint32_t)wrap1(my + dy, g.gy)) * gx;
-            const uint32_t A = W.start[base + mxlo - 1], B = W.start[base + mxhi + 2];
-            uint32_t a = 0u, b = 0u;
-            if (need) {
-                a = W.start[base + s.mx - 1];
-                b = W.start[base + s.mx + 2];
-            }
-            const float hx = need ? fmaf(sqrtf(w2), 1.0000009536743164f, xpad) : 0.f;
-            const float xlo = pi.x - hx, xhi = pi.x + hx;
-            bool done = !need || a == b;
-#pragma unroll 1
-            for (uint32_t c0 = A; c0 < B; c0 += kCoopChunk) {
-                const uint32_t m = min(kCoopChunk, B - c0);
-                for (uint32_t k = lane; k < m; k += 32u) {
-                    const uint32_t j = kInd ? G.order[c0 + k] : c0 + k;
-                    sm.pos[k] = G.pos[j];
-                    if (kInd) sm.idx[k] = j;
-                }
-                __syncwarp();
-                if (!done && b > c0 && a < c0 + m)
-                    done = density_scan<kInd>(sm, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo, xhi,
-                                              W.xmono, pi, W.h2, t, ks, kc, cnt, lrow, lcap);
-                __syncwarp();
-            }
+    for (int r = 0; r < 9; ++r) {
+        const float w2 = row_w2(W.h2w, ey2m, ey2p, ez2m, ez2p, r);
+        const bool need = fast && w2 > 0.f;
+        if (!__any_sync(0xffffffffu, need)) continue;
+        const uint32_t base = row_base(g, my, mz, r);
+        const uint32_t A = W.start[base + mxlo - 1], B = W.start[base + mxhi + 2];
+        uint32_t a = 0u, b = 0u;
+        if (need) {
+            a = W.start[base + s.mx - 1];
+            b = W.start[base + s.mx + 2];
         }
+        const float hx = need ? fmaf(sqrtf(w2), 1.0000009536743164f, xpad) : 0.f;
+        const float xlo = pi.x - hx, xhi = pi.x + hx;
+        bool done = !need || a == b;
+        float rs = 0.f;
+#pragma unroll 1
+        for (uint32_t c0 = A; c0 < B; c0 += kCoopChunk) {
+            const uint32_t m = min(kCoopChunk, B - c0);
+            for (uint32_t k = lane; k < m; k += 32u) {
+                const uint32_t j = kInd ? G.order[c0 + k] : c0 + k;
+                sm.pos[k] = G.pos[j];
+                if (kInd) sm.idx[k] = j;
+            }
+            __syncwarp();
+            if (!done && b > c0 && a < c0 + m)
+                done = density_scan<kInd>(sm, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo, xhi,
+                                          W.xmono, pi, W.h2, t, rs, cnt, lrow, lcap);
+            __syncwarp();
+        }
+        kahan_add(ks, kc, rs);
     }
     if (fast) density_finish(P, ks, cnt, lrow != nullptr, i, pi, vel, rp, fr, L);
 }
