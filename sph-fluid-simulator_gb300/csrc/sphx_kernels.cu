@@ -1155,24 +1155,58 @@ __device__ __forceinline__ void density_finish(const StepParams &P, float acc, u
     }
 }
 
+// The density pass's chunk of a neighbour row: cell-sorted positions c0,
+// c0 + 1, ... as three coordinate arrays (so that two neighbouring
+// candidates' coordinates load as one 8-byte pair), and with kInd their
+// particle indices.
+template <bool kInd>
+struct DensityChunk {
+    __align__(16) float x[kCoopChunk];
+    __align__(16) float y[kCoopChunk];
+    __align__(16) float z[kCoopChunk];
+    uint32_t idx[kInd ? kCoopChunk : 1];
+};
+
+// Two FP32 values in one 64-bit register pair, and the packed
+// round-to-nearest arithmetic on them (each half rounded on its own, as
+// __fsub_rn / __fmul_rn / __fadd_rn round it).
+__device__ __forceinline__ uint64_t f32x2_dup(float v) {
+    const uint64_t b = __float_as_uint(v);
+    return b | (b << 32);
+}
+__device__ __forceinline__ float f32x2_lo(uint64_t v) { return __uint_as_float((uint32_t)v); }
+__device__ __forceinline__ float f32x2_hi(uint64_t v) { return __uint_as_float((uint32_t)(v >> 32)); }
+__device__ __forceinline__ uint64_t f32x2_sub(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f32x2_mul(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f32x2_add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // One lane's scan of chunk slots [lo, hi) of a neighbour row (the chunk
 // holds cell-sorted positions c0, c0 + 1, ...): every candidate inside the
 // lane's x window is tested with the reference's float r^2 (sph.cpp:57: (dx*dx
-// + dy*dy) + dz*dz, no fused multiply-add); an accepted one adds
-// (h^2 - r^2)^3 to the row's sum rs (one fused multiply-add) and its index
-// to the list row (while it has room).  x-sorted runs (xmono): start at the
-// first x >= xlo (binary search), stop at the first x > xhi; returns true
-// once past the window.  Otherwise every slot is checked against the window.
+// + dy*dy) + dz*dz, no fused multiply-add; two candidates at a time in
+// packed pairs, each rounded as alone); an accepted one adds (h^2 - r^2)^3
+// to the row's sum rs (one fused multiply-add) and its index to the list row
+// (while it has room).  x-sorted runs (xmono): start at the first x >= xlo
+// (binary search), stop at the first x > xhi; returns true once past the
+// window.  Otherwise every slot is checked against the window.
 template <bool kInd>
-__device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c0, uint32_t lo,
+__device__ __forceinline__ bool density_scan(const DensityChunk<kInd> &sm, uint32_t c0, uint32_t lo,
                                              uint32_t hi, float xlo, float xhi, bool xmono,
                                              float4 pi, float h2, uint32_t self, float &rs,
                                              uint32_t &cnt, uint32_t *lrow, uint32_t lcap) {
-    auto visit = [&](uint32_t k, float4 p) {
-        const float dx = __fsub_rn(p.x, pi.x);
-        const float dy = __fsub_rn(p.y, pi.y);
-        const float dz = __fsub_rn(p.z, pi.z);
-        const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    auto accept = [&](uint32_t k, float d2) {
         if (d2 < h2 && c0 + k != self) {
             const float u = __fsub_rn(h2, d2);
             rs = __fmaf_rn(__fmul_rn(u, u), u, rs);
@@ -1182,24 +1216,49 @@ __device__ __forceinline__ bool density_scan(const PosSmem<kInd> &sm, uint32_t c
             ++cnt;
         }
     };
+    auto one = [&](uint32_t k, float px) {
+        const float dx = __fsub_rn(px, pi.x);
+        const float dy = __fsub_rn(sm.y[k], pi.y);
+        const float dz = __fsub_rn(sm.z[k], pi.z);
+        accept(k, __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    };
     if (!xmono) {
         for (uint32_t k = lo; k < hi; ++k) {
-            const float4 p = sm.pos[k];
-            if (p.x >= xlo && p.x <= xhi) visit(k, p);
+            const float px = sm.x[k];
+            if (px >= xlo && px <= xhi) one(k, px);
         }
         return false;
     }
-    uint32_t l = lo, u = hi;
-    while (l < u) {
-        const uint32_t mid = (l + u) >> 1;
-        if (sm.pos[mid].x < xlo) l = mid + 1;
+    uint32_t k = lo, u = hi;
+    while (k < u) {
+        const uint32_t mid = (k + u) >> 1;
+        if (sm.x[mid] < xlo) k = mid + 1;
         else u = mid;
     }
-#pragma unroll kScanUnroll
-    for (uint32_t k = l; k < hi; ++k) {
-        const float4 p = sm.pos[k];
-        if (p.x > xhi) return true;
-        visit(k, p);
+    if ((k & 1u) && k < hi) {  // pairs start at even slots
+        const float px = sm.x[k];
+        if (px > xhi) return true;
+        one(k, px);
+        ++k;
+    }
+    const uint64_t PX = f32x2_dup(pi.x), PY = f32x2_dup(pi.y), PZ = f32x2_dup(pi.z);
+#pragma unroll 2
+    for (; k + 1u < hi; k += 2u) {
+        const uint64_t X = *reinterpret_cast<const uint64_t *>(sm.x + k);
+        if (f32x2_lo(X) > xhi) return true;
+        const uint64_t Y = *reinterpret_cast<const uint64_t *>(sm.y + k);
+        const uint64_t Z = *reinterpret_cast<const uint64_t *>(sm.z + k);
+        const uint64_t dX = f32x2_sub(X, PX), dY = f32x2_sub(Y, PY), dZ = f32x2_sub(Z, PZ);
+        const uint64_t D2 =
+            f32x2_add(f32x2_add(f32x2_mul(dX, dX), f32x2_mul(dY, dY)), f32x2_mul(dZ, dZ));
+        accept(k, f32x2_lo(D2));
+        if (f32x2_hi(X) > xhi) return true;
+        accept(k + 1u, f32x2_hi(D2));
+    }
+    if (k < hi) {
+        const float px = sm.x[k];
+        if (px > xhi) return true;
+        one(k, px);
     }
     return false;
 }
@@ -1229,7 +1288,7 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     k_density(SceneTable T, WalkCtx G, const float4 *__restrict__ vel, float4 *__restrict__ rp,
               float4 *__restrict__ fr, NbrList L, RowWarps RW, uint32_t *__restrict__ deferred,
               uint32_t *__restrict__ status) {
-    __shared__ PosSmem<kInd> s_chunk[kThreads / 32];
+    __shared__ DensityChunk<kInd> s_chunk[kThreads / 32];
     if (status[0] & kStatusErrorMask) return;
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1268,7 +1327,7 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     const uint32_t lcap = lrow ? L.slots : 0u;
     float ks = 0.f, kc = 0.f;
     uint32_t cnt = 0u;
-    PosSmem<kInd> &sm = s_chunk[threadIdx.x >> 5];
+    DensityChunk<kInd> &sm = s_chunk[threadIdx.x >> 5];
 #pragma unroll 1
     for (int r = 0; r < 9; ++r) {
         const float w2 = row_w2(W.h2w, ey2m, ey2p, ez2m, ez2p, r);
@@ -1290,7 +1349,10 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
             const uint32_t m = min(kCoopChunk, B - c0);
             for (uint32_t k = lane; k < m; k += 32u) {
                 const uint32_t j = kInd ? G.order[c0 + k] : c0 + k;
-                sm.pos[k] = G.pos[j];
+                const float4 p = G.pos[j];
+                sm.x[k] = p.x;
+                sm.y[k] = p.y;
+                sm.z[k] = p.z;
                 if (kInd) sm.idx[k] = j;
             }
             __syncwarp();
