@@ -330,18 +330,28 @@ def run_serve(a):
 
 
 def run_steps_only(a):
-    """Profiling driver: the headline scene (or a --side^3 block), W + K steps
+    """Profiling driver: the headline scene (or a --side^3 block, or with
+    --scenes the batched workload's first N scenes as one batch), W + K steps
     as plain launches (no graph, no events), one summary line."""
     import torch
     import sphx
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    pos, box = sphx.dambreak(a.side)
-    with sphx.Scene(sphx.config_settings(), box, pos, None,
-                    sphx.default_options(device=local, use_graph=0)) as sc:
-        sc.step(sphx.DT, a.warmup + a.steps)
-        sc.synchronize()
-    print(json.dumps({"workload": "steps", "particles": len(pos), "steps": a.warmup + a.steps}))
+    opt = sphx.default_options(device=local, use_graph=0)
+    if a.scenes:
+        scenes = sphx.batch_scenes(a.scenes, seed=0)
+        n = sum(len(p) for _, p, _ in scenes)
+        with sphx.Scene.batch(scenes, opt) as b:
+            b.step(sphx.DT, a.warmup + a.steps)
+            b.synchronize()
+    else:
+        pos, box = sphx.dambreak(a.side)
+        n = len(pos)
+        with sphx.Scene(sphx.config_settings(), box, pos, None, opt) as sc:
+            sc.step(sphx.DT, a.warmup + a.steps)
+            sc.synchronize()
+    print(json.dumps({"workload": "steps", "scenes": a.scenes or 1, "particles": n,
+                      "steps": a.warmup + a.steps}))
 
 
 def run_reference(a):
@@ -635,6 +645,8 @@ def main():
     ap.add_argument("--impl", default="sphx", choices=["sphx", "reference"])
     ap.add_argument("--workload", default="plain", choices=["plain", "batch", "serve", "steps"])
     ap.add_argument("--side", type=int, default=SIDE, help="block side of --workload steps")
+    ap.add_argument("--scenes", type=int, default=0,
+                    help="--workload steps: step the batched workload's first N scenes instead")
     ap.add_argument("--batch-steps", type=int, default=200,
                     help="steps of the batched-vs-sequential comparison in the plain run (0: skip)")
     ap.add_argument("--requests", type=int, default=64,
