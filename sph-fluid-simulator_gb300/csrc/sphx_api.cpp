@@ -170,7 +170,7 @@ Layout layout_for(size_t cn, size_t cs, size_t csc, size_t slots) {
                                         4 * (cs + 1), 4 * (cs + 1), 4 * ntiles, 256, 24 * cn,
                                         sizeof(sphx::StepParams) * csc, 4 * (csc + 1),
                                         4 * (csc + 1), 8ull * sphx::large_list_cap((uint32_t)cn),
-                                        32 * cn, 4ull * slots * cn, 4 * cn, 8 * cn,
+                                        32 * cn, 4ull * slots * ((cn + 31) / 32 * 32), 4 * cn, 8 * cn,
                                         4 * (csc + 1), 4 * (cs + 1), 8 * cn + 4 * (cn / 32 + 1),
                                         cs + 1};
     Layout L;

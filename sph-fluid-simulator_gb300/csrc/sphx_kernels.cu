@@ -1073,23 +1073,33 @@ __device__ __forceinline__ void kahan_add_cube(float &s, float &c, float u) {
     s = t;
 }
 
+// Neighbour lists in tiles of 32 cell-sorted slots (a force warp's
+// particles), four entries per slot side by side: entry k of slot t is
+// nbr[(t / 32) * slots * 32 + (k / 4) * 128 + (t % 32) * 4 + k % 4], so that
+// a force warp's 16-byte load of entries k..k+3 of its 32 slots reads 512
+// contiguous bytes instead of 32 rows' lines.  list_base(L, t) is the address
+// of entry 0 of slot t, list_offset(k) the offset of entry k from it.
+__device__ __forceinline__ uint32_t *list_base(const NbrList &L, uint32_t t) {
+    return L.nbr + (size_t)(t >> 5) * L.slots * 32u + (t & 31u) * 4u;
+}
+__device__ __forceinline__ uint32_t list_offset(uint32_t k) { return k + (k & ~3u) * 31u; }
+
 // Accepted neighbours of a particle, in walk order, are also recorded for
-// the force kernel: entry k of particle i is nbr[i * slots + k], k < slots
-// (one contiguous row per particle, written by one lane front to back); a
-// particle with more (clumped fluid), or of a crowded cell, stores its count
-// only and the force kernel walks for it instead.
+// the force kernel (list_base: k < slots, written by one lane front to
+// back); a particle with more (clumped fluid), or of a crowded cell, stores
+// its count only and the force kernel walks for it instead.
 struct DensityVisitor {
     __device__ __forceinline__ void on_test() {}
     float h2;
     float acc, comp;  // compensated sum of (h^2 - r^2)^3
-    uint32_t *row;    // &nbr[i * slots], or NULL: nothing recorded
+    uint32_t *row;    // list_base of the particle's slot, or NULL: nothing recorded
     uint32_t slots;
     uint32_t cnt;
     __device__ __forceinline__ void operator()(uint32_t j, float, float, float, float d2) {
         kahan_add_cube(acc, comp, __fsub_rn(h2, d2));
         // streaming store: the force pass reads the row once, after every
         // other row has been written
-        if (row && cnt < slots) __stcs(row + cnt, j);
+        if (row && cnt < slots) __stcs(row + list_offset(cnt), j);
         ++cnt;
     }
 };
@@ -1126,12 +1136,12 @@ constexpr uint32_t kNoList = 0x80000000u;
 // force pass walks for it: recording them would only cost writes.  Either
 // way the force is the same.
 __device__ __forceinline__ uint32_t *density_row(const WalkCtx &W, const WalkStart &s,
-                                                 const NbrList &L, uint32_t i) {
+                                                 const NbrList &L, uint32_t t) {
     if (!L.nbr) return nullptr;
     const uint32_t k = ((uint32_t)s.mz * (uint32_t)W.grid.gy + (uint32_t)s.my) *
                            (uint32_t)W.grid.gx + (uint32_t)s.mx;
     const uint32_t occ = W.start[k + 1] - W.start[k];
-    return occ * kListSkipFactor <= L.slots ? L.nbr + (size_t)i * L.slots : nullptr;
+    return occ * kListSkipFactor <= L.slots ? list_base(L, t) : nullptr;
 }
 
 // Density, pressure, the list count and the neighbour record of particle i
@@ -1212,7 +1222,7 @@ __device__ __forceinline__ bool density_scan(const DensityChunk<kInd> &sm, uint3
             rs = __fmaf_rn(__fmul_rn(u, u), u, rs);
             // streaming store: the force pass reads the row once, after
             // every other row has been written
-            if (cnt < lcap) __stcs(lrow + cnt, kInd ? sm.idx[k] : c0 + k);
+            if (cnt < lcap) __stcs(lrow + list_offset(cnt), kInd ? sm.idx[k] : c0 + k);
             ++cnt;
         }
     };
@@ -1323,7 +1333,7 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
     ez2m *= ez2m;
     ez2p *= ez2p;
     const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
-    uint32_t *lrow = fast ? density_row(W, s, L, i) : nullptr;
+    uint32_t *lrow = fast ? density_row(W, s, L, t) : nullptr;
     const uint32_t lcap = lrow ? L.slots : 0u;
     float ks = 0.f, kc = 0.f;
     uint32_t cnt = 0u;
@@ -1386,7 +1396,7 @@ __global__ void __launch_bounds__(kDeferredThreads)
         const float4 pi = W.pos[i];
         WalkStart s;
         walk_start(W, P, pi, s);
-        DensityVisitor v{P.h2, 0.f, 0.f, lane == 0 ? density_row(W, s, L, i) : nullptr, L.slots, 0u};
+        DensityVisitor v{P.h2, 0.f, 0.f, lane == 0 ? density_row(W, s, L, t) : nullptr, L.slots, 0u};
         PosScan<kInd, DensityVisitor> scan{s_chunk[threadIdx.x >> 5], v};
         warp_walk<kInd>(W, s, i, pi, scan);
         if (lane == 0) density_finish(P, v.acc, v.cnt, v.row != nullptr, i, pi, vel, rp, fr, L);
@@ -1631,12 +1641,13 @@ __global__ void __launch_bounds__(kThreads, kForceListThreadsPerSM / kThreads)
     const float4 vi = vel[i];
     const float4 q = rp[i];
     ForcePair pair{vi, q.y, P.h, P.forceKp, P.forceKv, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    // the row is 16-byte aligned (slots is a multiple of 4): four entries per
-    // load; entries past cnt in the last load are never used
-    const uint4 *row = reinterpret_cast<const uint4 *>(L.nbr + (size_t)i * L.slots);
+    // four entries per 16-byte load, the warp's 32 slots side by side
+    // (list_base): one load of the warp reads 512 contiguous bytes; entries
+    // past cnt in the last load are never used
+    const uint4 *row = reinterpret_cast<const uint4 *>(list_base(L, t));
 #pragma unroll 1
     for (uint32_t k = 0; k < cnt; k += 4) {
-        const uint4 e = row[k >> 2];
+        const uint4 e = row[(k >> 2) * 32u];
         const uint32_t left = cnt - k;
         {  // two records in flight, then summed in list order
             const uint32_t j1 = left > 1 ? e.y : e.x;

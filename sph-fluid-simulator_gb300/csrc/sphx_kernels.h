@@ -65,10 +65,13 @@ cudaError_t prepare_device();
 cudaError_t launch_gather(uint32_t n, const SortBuffers &B, const float4 *pos_in,
                           const float4 *vel_in, const uint32_t *id_in, float4 *pos_out,
                           float4 *vel_out, uint32_t *id_out, cudaStream_t st);
-// Accepted-neighbour lists the density kernel records for the force kernel:
-// entry k of particle i is nbr[i * slots + k] for k < min(count[i], slots),
-// slots a multiple of 4; a count above `slots` means the force kernel walks
-// for that particle.  nbr NULL: nothing is recorded (the density pass alone).
+// Accepted-neighbour lists the density kernel records for the force kernel,
+// in tiles of 32 cell-sorted slots: entry k < min(count[i], slots) of the
+// particle at slot t is nbr[(t / 32) * slots * 32 + (k / 4) * 128 +
+// (t % 32) * 4 + k % 4] (nbr holds slots entries for every slot, n rounded
+// up to 32), slots a multiple of 4; a count above `slots` means the force
+// kernel walks for that particle.  nbr NULL: nothing is recorded (the
+// density pass alone).
 struct NbrList {
     uint32_t *nbr;
     uint32_t *count;
