@@ -195,7 +195,9 @@ int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3);
 int sphx_step(sphx_handle *h, float dt, int nsteps);
 int sphx_synchronize(sphx_handle *h);
 /* Host readout in id order; any pointer may be NULL.  force3 / rho / prs are
- * the values of the last step (what it integrated with). */
+ * the values of the last step (what it integrated with).  Waits for the
+ * queued steps; if one of them stopped on an error, returns that error and
+ * the arrays' contents are unspecified. */
 int sphx_read_state(sphx_handle *h, float *pos3, float *vel3, float *rho, float *prs,
                     float *force3);
 /* translate(position) * scale(h/2) per particle, 16 floats column-major, id

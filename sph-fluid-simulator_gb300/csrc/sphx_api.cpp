@@ -279,6 +279,32 @@ int upload_scene(sphx_handle *h, const sphx::Scene &sc, const float *pos3, const
     return SPHX_OK;
 }
 
+// sphx_set_state's upload of one scene, in two halves.  The first puts the
+// copies into staging on the copy stream, once the kernels queued before
+// have released staging; the second queues the upload kernel on the kernel
+// stream behind the copies.  Work queued on the kernel stream between the
+// two runs beside the copies.  No host wait (the caller synchronises).
+int upload_copies(sphx_handle *h, const sphx::Scene &sc, const float *pos3, const float *vel3) {
+    const size_t n = sc.n;
+    float *sp = h->staging, *sv = h->staging + 3 * (size_t)h->cap_n;
+    SPHX_CUDA(cudaEventRecord(h->ev_kernels, h->stream));
+    SPHX_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_kernels, 0));
+    SPHX_CUDA(cudaMemcpyAsync(sp, pos3, 12 * n, cudaMemcpyHostToDevice, h->copy_stream));
+    if (vel3) SPHX_CUDA(cudaMemcpyAsync(sv, vel3, 12 * n, cudaMemcpyHostToDevice, h->copy_stream));
+    else SPHX_CUDA(cudaMemsetAsync(sv, 0, 12 * n, h->copy_stream));
+    SPHX_CUDA(cudaEventRecord(h->ev_copies, h->copy_stream));
+    return SPHX_OK;
+}
+
+int upload_rows_after_copies(sphx_handle *h, const sphx::Scene &sc, uint32_t *bad, bool keep_order) {
+    float *sp = h->staging, *sv = h->staging + 3 * (size_t)h->cap_n;
+    SPHX_CUDA(cudaStreamWaitEvent(h->stream, h->ev_copies, 0));
+    SPHX_CUDA(sphx::launch_upload_rows(sc.first, sc.n, sp, sv, h->pos[h->pv], h->vel[h->pv],
+                                       h->id[h->idc], sc.d.h, bad, keep_order, h->sb.status,
+                                       h->stream));
+    return SPHX_OK;
+}
+
 // Lattice corners (jitter included) as two points, for the grid choice and
 // the domain check.
 void lattice_corners(const sphx_lattice_desc &L, float *pts) {
@@ -547,6 +573,12 @@ int sphx::create_handle(const SceneInit *inits, size_t nscenes, const sphx_optio
         }
         h->own_stream = true;
     }
+    if (cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_kernels, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_copies, cudaEventDisableTiming) != cudaSuccess) {
+        sphx_destroy(h);
+        return fail(SPHX_ERR_CUDA, "copy stream creation failed");
+    }
     char *arena = nullptr;
     Layout L;
     int rc = alloc_arena(h, h->cap_n, h->cap_slots, h->cap_scenes, &arena, &L);
@@ -776,11 +808,15 @@ int sphx_destroy(sphx_handle *h) {
     if (!h) return SPHX_OK;
     cudaSetDevice(h->opt.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->copy_stream) cudaStreamSynchronize(h->copy_stream);
     sphx::destroy_graphs(h);
     for (cudaEvent_t e : h->events) cudaEventDestroy(e);
     if (h->transforms) cudaFree(h->transforms);
     if (h->arena) cudaFree(h->arena);
     if (h->h_status) cudaFreeHost(h->h_status);
+    if (h->ev_kernels) cudaEventDestroy(h->ev_kernels);
+    if (h->ev_copies) cudaEventDestroy(h->ev_copies);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return SPHX_OK;
@@ -810,14 +846,23 @@ int sphx_set_state(sphx_handle *h, const float *pos3, const float *vel3) {
     // error bits itself).
     const bool keep = h->error == 0;
     SPHX_CUDA(cudaMemsetAsync(bad, 0xFF, 4, h->stream));
-    for (const sphx::Scene &sc : h->scenes) {
-        const int rc = upload_scene(h, sc, pos3 + 3ull * sc.first,
-                                    vel3 ? vel3 + 3ull * sc.first : nullptr, h->pv, h->idc, bad, keep);
-        if (rc) return rc;
+    for (size_t k = 0; k < h->scenes.size(); ++k) {
+        const sphx::Scene &sc = h->scenes[k];
+        int rc = upload_copies(h, sc, pos3 + 3ull * sc.first, vel3 ? vel3 + 3ull * sc.first : nullptr);
+        // the last step's outputs are cleared while the first scene's
+        // copies run
+        if (rc == SPHX_OK && k == 0 && cudaMemsetAsync(h->rp, 0, 16ull * h->n, h->stream) != cudaSuccess)
+            rc = fail(SPHX_ERR_CUDA, "clearing densities failed");
+        if (rc == SPHX_OK && k == 0 && cudaMemsetAsync(h->force, 0, 16ull * h->n, h->stream) != cudaSuccess)
+            rc = fail(SPHX_ERR_CUDA, "clearing forces failed");
+        if (rc == SPHX_OK) rc = upload_rows_after_copies(h, sc, bad, keep);
+        if (rc) {
+            cudaStreamSynchronize(h->copy_stream);
+            cudaStreamSynchronize(h->stream);
+            return rc;
+        }
     }
     SPHX_CUDA(cudaMemsetAsync(h->sb.status, 0, 8, h->stream));
-    SPHX_CUDA(cudaMemsetAsync(h->rp, 0, 16ull * h->n, h->stream));
-    SPHX_CUDA(cudaMemsetAsync(h->force, 0, 16ull * h->n, h->stream));
     SPHX_CUDA(cudaMemcpyAsync(h->h_status, bad, 4, cudaMemcpyDeviceToHost, h->stream));
     SPHX_CUDA(cudaStreamSynchronize(h->stream));
     const uint32_t row = *h->h_status;
@@ -850,8 +895,8 @@ int sphx_synchronize(sphx_handle *h) {
 
 int sphx_read_state(sphx_handle *h, float *pos3, float *vel3, float *rho, float *prs,
                     float *force3) {
-    const int rc = sphx_synchronize(h);
-    if (rc) return rc;
+    HANDLE_CHECK(h);
+    if (h->error) return fail(h->error, "handle is in an error state; call sphx_set_state");
     const size_t n = h->n;
     const sphx::SceneTable T = sphx::table_of(h);
     struct F {
@@ -864,23 +909,45 @@ int sphx_read_state(sphx_handle *h, float *pos3, float *vel3, float *rho, float 
                   {force3, 2, h->force, 3 * n},
                   {rho, 3, nullptr, n},
                   {prs, 4, nullptr, n}};
-    // fields share the staging area (6 floats per particle of capacity) and
-    // wait only when it is full
+    // Each field is gathered into id order in staging on the kernel stream
+    // (behind the queued steps) and copied out on the copy stream, so that
+    // one field's copy runs beside the next field's gather.  Fields share
+    // staging (6 floats per particle of capacity) and wait only when it is
+    // full.  The step's status word comes back last; a step that stopped on
+    // an error makes the call return that error (the arrays then hold
+    // whatever the failed state gave).
     const size_t cap = 6ull * h->cap_n;
     size_t used = 0;
+    int rc = SPHX_OK;
     for (const F &f : fields) {
         if (!f.dst) continue;
         if (used + f.floats > cap) {
-            SPHX_CUDA(cudaStreamSynchronize(h->stream));
+            if (cudaStreamSynchronize(h->copy_stream) != cudaSuccess) {
+                rc = fail(SPHX_ERR_CUDA, "readout copy failed");
+                break;
+            }
             used = 0;
         }
         float *out = h->staging + used;
-        SPHX_CUDA(sphx::launch_read_field(T, f.field, h->id[h->idc], f.src, h->rp, out, h->stream));
-        SPHX_CUDA(cudaMemcpyAsync(f.dst, out, 4 * f.floats, cudaMemcpyDeviceToHost, h->stream));
+        if (sphx::launch_read_field(T, f.field, h->id[h->idc], f.src, h->rp, out, h->sb.status,
+                                    h->stream) !=
+                cudaSuccess ||
+            cudaEventRecord(h->ev_kernels, h->stream) != cudaSuccess ||
+            cudaStreamWaitEvent(h->copy_stream, h->ev_kernels, 0) != cudaSuccess ||
+            cudaMemcpyAsync(f.dst, out, 4 * f.floats, cudaMemcpyDeviceToHost, h->copy_stream) !=
+                cudaSuccess) {
+            rc = fail(SPHX_ERR_CUDA, "readout failed");
+            break;
+        }
         used += f.floats;
     }
-    SPHX_CUDA(cudaStreamSynchronize(h->stream));
-    return SPHX_OK;
+    const cudaError_t e1 = cudaStreamSynchronize(h->copy_stream);
+    if (rc) {
+        cudaStreamSynchronize(h->stream);
+        return rc;
+    }
+    if (e1 != cudaSuccess) return fail(SPHX_ERR_CUDA, std::string("readout: ") + cudaGetErrorString(e1));
+    return sphx::read_status(h);
 }
 
 int sphx_read_scene(sphx_handle *h, size_t scene, float *pos3, float *vel3, float *rho,

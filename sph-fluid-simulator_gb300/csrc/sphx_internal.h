@@ -60,6 +60,10 @@ struct sphx_handle {
     uint32_t cap_n = 0, cap_slots = 0, cap_scenes = 0;  // arena capacities
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // host <-> device copies of sphx_set_state / sphx_read_state, beside the
+    // kernels on `stream`; both streams are idle when either call returns
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_kernels = nullptr, ev_copies = nullptr;
     char *arena = nullptr;
     float4 *pos[2] = {nullptr, nullptr};
     float4 *vel[2] = {nullptr, nullptr};
@@ -67,7 +71,7 @@ struct sphx_handle {
     float4 *rp = nullptr;                  // density, pressure, 1/density, 0
     float4 *force = nullptr;
     float4 *fr = nullptr;         // 32-byte neighbour records (density -> force)
-    uint32_t *nbr = nullptr;      // accepted-neighbour lists, 64 rows of cap_n
+    uint32_t *nbr = nullptr;      // accepted-neighbour lists (tiles of 32 slots, see sphx_kernels.h)
     uint32_t *ncount = nullptr;   // accepted-neighbour count per particle
     float *staging = nullptr;     // 6 floats per particle of capacity
     float *transforms = nullptr;  // 16 floats per particle, allocated on first use

@@ -1887,10 +1887,14 @@ __global__ void k_read_rows(uint32_t first, uint32_t n, int field, const uint32_
 // scalars.  field: 0 pos, 1 vel, 2 force, 3 rho, 4 prs.
 __global__ void k_read_field(SceneTable T, int field, const uint32_t *__restrict__ id,
                              const float4 *__restrict__ v4, const float4 *__restrict__ rp,
-                             float *__restrict__ out) {
+                             float *__restrict__ out, const uint32_t *__restrict__ status) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= T.n) return;
-    const uint32_t d = T.pofs[scene_of(T, i)] + id[i];
+    // after a failed step the ids need not be a permutation: write nothing
+    if (i >= T.n || (status[0] & kStatusErrorMask)) return;
+    const uint32_t sc = scene_of(T, i);
+    const uint32_t first = T.pofs[sc], local = id[i];
+    if (local >= T.pofs[sc + 1] - first) return;
+    const uint32_t d = first + local;
     if (field <= 2) {
         const float4 v = v4[i];
         out[3 * d] = v.x;
@@ -2188,8 +2192,9 @@ cudaError_t launch_read_rows(uint32_t first, uint32_t n, int field, const uint32
 }
 
 cudaError_t launch_read_field(const SceneTable &T, int field, const uint32_t *id, const float4 *v4,
-                              const float4 *rp, float *out, cudaStream_t st) {
-    if (T.n) k_read_field<<<blocks(T.n, 256), 256, 0, st>>>(T, field, id, v4, rp, out);
+                              const float4 *rp, float *out, const uint32_t *status,
+                              cudaStream_t st) {
+    if (T.n) k_read_field<<<blocks(T.n, 256), 256, 0, st>>>(T, field, id, v4, rp, out, status);
     return cudaGetLastError();
 }
 

@@ -122,8 +122,12 @@ cudaError_t launch_lattice_rows(uint32_t first, const LatticeGen &L, float4 *pos
                                 uint32_t *id, cudaStream_t st);
 cudaError_t launch_read_rows(uint32_t first, uint32_t n, int field, const uint32_t *id,
                              const float4 *v4, const float4 *rp, float *out, cudaStream_t st);
+// All scenes' rows to staging in id order; writes nothing when the sticky
+// error bits of status (word 0) are set, and skips a row whose id is out of
+// its scene's range.
 cudaError_t launch_read_field(const SceneTable &T, int field, const uint32_t *id, const float4 *v4,
-                              const float4 *rp, float *out, cudaStream_t st);
+                              const float4 *rp, float *out, const uint32_t *status,
+                              cudaStream_t st);
 cudaError_t launch_transforms(const SceneTable &T, const uint32_t *id, const float4 *pos,
                               float *out16, cudaStream_t st);
 cudaError_t launch_cells(const SceneTable &T, const uint32_t *id, const float4 *pos, int *cells,
