@@ -436,12 +436,15 @@ __device__ __forceinline__ int wrap1(int v, int m) {
 }
 
 // The nine (dy, dz) neighbour rows of a cell, in the order every walk
-// visits them: the dz = 0 layer, then dz = +1, then dz = -1, each as
-// dy = -1, 0, +1.  (k_density takes the first three as one group and the
-// last six as another: the z layers on either side of a particle hold
-// complementary x windows, so a lane's work over the pair varies little.)
+// visits them (and the neighbour lists record them): the dz = 0 layer, then
+// dz = +1, then dz = -1, each as dy = 0, -1, +1.  The particle's own row and
+// layer come first: their neighbours are the ones the neighbouring lanes of
+// a force warp gather too.
 __device__ __forceinline__ int row_dz(int r) { return r < 3 ? 0 : (r < 6 ? 1 : -1); }
-__device__ __forceinline__ int row_dy(int r) { return r % 3 - 1; }
+__device__ __forceinline__ int row_dy(int r) {
+    const int q = r % 3;
+    return q == 0 ? 0 : (q == 1 ? -1 : 1);
+}
 
 // Fast path: the 27 cells around (mx, my, mz), each visited once.
 __device__ __forceinline__ uint32_t row_base(const Grid &g, int my, int mz, int r) {
@@ -501,7 +504,7 @@ __device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, in
         uint32_t rows = 0;
 #pragma unroll
         for (int r = 0; r < 9; ++r)
-            if (W.h2w - ey2[r % 3] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
+            if (W.h2w - ey2[row_dy(r) + 1] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
         const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
         int r = __ffs(rows) - 1;
         rows &= rows - 1;
@@ -518,7 +521,7 @@ __device__ __forceinline__ void walk_rows(const WalkCtx &W, const CellPos &c, in
                 a = W.start[base + mx - 1];
                 b = W.start[base + mx + 2];
             }
-            const int iy = cr % 3, iz = row_dz(cr) + 1;
+            const int iy = row_dy(cr) + 1, iz = row_dz(cr) + 1;
             const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
             const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
             const float hx = fmaf(sqrtf(W.h2w - eyy - ezz), 1.0000009536743164f, xpad);
@@ -687,7 +690,7 @@ __device__ __forceinline__ void coop_rows_group(const WalkCtx &W, const WalkStar
     uint32_t rows = 0;
 #pragma unroll
     for (int r = 0; r < 9; ++r)
-        if (W.h2w - ey2[r % 3] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
+        if (W.h2w - ey2[row_dy(r) + 1] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
     const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
     uint32_t todo = __reduce_or_sync(gmask, rows);
     const uint32_t mxlo = __reduce_min_sync(gmask, (uint32_t)s.mx);
@@ -700,7 +703,7 @@ __device__ __forceinline__ void coop_rows_group(const WalkCtx &W, const WalkStar
         const uint32_t base = row_base(W.grid, s.my, s.mz, r);
         const uint32_t A = W.start[base + mxlo - 1], B = W.start[base + mxhi + 2];
         const uint32_t a = W.start[base + s.mx - 1], b = W.start[base + s.mx + 2];
-        const int iy = r % 3, iz = row_dz(r) + 1;
+        const int iy = row_dy(r) + 1, iz = row_dz(r) + 1;
         const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
         const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
         bool done = !((rows >> r) & 1u) || a == b;
@@ -737,7 +740,7 @@ __device__ __forceinline__ void coop_rows_warp(const WalkCtx &W, const WalkStart
         ez2[2] = ezp * ezp;
 #pragma unroll
         for (int r = 0; r < 9; ++r)
-            if (W.h2w - ey2[r % 3] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
+            if (W.h2w - ey2[row_dy(r) + 1] - ez2[row_dz(r) + 1] > 0.f) rows |= 1u << r;
     }
     const float xpad = fabsf(pi.x) * 2.384185791015625e-07f;  // |x| 2^-22
     uint32_t todo = __reduce_or_sync(0xffffffffu, rows);
@@ -757,7 +760,7 @@ __device__ __forceinline__ void coop_rows_warp(const WalkCtx &W, const WalkStart
         }
         A = __shfl_sync(0xffffffffu, A, leader);
         B = __shfl_sync(0xffffffffu, B, leader);
-        const int iy = r % 3, iz = row_dz(r) + 1;
+        const int iy = row_dy(r) + 1, iz = row_dz(r) + 1;
         const float eyy = iy == 0 ? ey2[0] : (iy == 2 ? ey2[2] : 0.f);
         const float ezz = iz == 0 ? ez2[0] : (iz == 2 ? ez2[2] : 0.f);
         bool done = !member || !((rows >> r) & 1u) || a == b;
