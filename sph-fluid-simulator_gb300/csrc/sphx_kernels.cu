@@ -1213,14 +1213,16 @@ __device__ __forceinline__ uint64_t f32x2_add(uint64_t a, uint64_t b) {
 // to the row's sum rs (one fused multiply-add) and its index to the list row
 // (while it has room).  x-sorted runs (xmono): start at the first x >= xlo
 // (binary search), stop at the first x > xhi; returns true once past the
-// window.  Otherwise every slot is checked against the window.
-template <bool kInd>
+// window.  Otherwise every slot is checked against the window.  kSelf: the
+// particle's own row, the only one that holds the particle itself (skipped
+// by its cell-sorted position self).
+template <bool kInd, bool kSelf>
 __device__ __forceinline__ bool density_scan(const DensityChunk<kInd> &sm, uint32_t c0, uint32_t lo,
                                              uint32_t hi, float xlo, float xhi, bool xmono,
                                              float4 pi, float h2, uint32_t self, float &rs,
                                              uint32_t &cnt, uint32_t *lrow, uint32_t lcap) {
     auto accept = [&](uint32_t k, float d2) {
-        if (d2 < h2 && c0 + k != self) {
+        if (d2 < h2 && (!kSelf || c0 + k != self)) {
             const float u = __fsub_rn(h2, d2);
             rs = __fmaf_rn(__fmul_rn(u, u), u, rs);
             // streaming store: the force pass reads the row once, after
@@ -1369,9 +1371,14 @@ __global__ void __launch_bounds__(kThreads, kDensityThreadsPerSM / kThreads)
                 if (kInd) sm.idx[k] = j;
             }
             __syncwarp();
-            if (!done && b > c0 && a < c0 + m)
-                done = density_scan<kInd>(sm, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo, xhi,
-                                          W.xmono, pi, W.h2, t, rs, cnt, lrow, lcap);
+            if (!done && b > c0 && a < c0 + m) {
+                if (r == 0)
+                    done = density_scan<kInd, true>(sm, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo,
+                                                    xhi, W.xmono, pi, W.h2, t, rs, cnt, lrow, lcap);
+                else
+                    done = density_scan<kInd, false>(sm, c0, a > c0 ? a - c0 : 0u, min(b - c0, m), xlo,
+                                                     xhi, W.xmono, pi, W.h2, t, rs, cnt, lrow, lcap);
+            }
             __syncwarp();
         }
         kahan_add(ks, kc, rs);
