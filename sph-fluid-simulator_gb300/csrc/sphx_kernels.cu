@@ -1282,9 +1282,11 @@ __device__ __forceinline__ bool density_scan(const DensityChunk<kInd> &sm, uint3
 // warps k_row_warps counted).  The reference accumulates m*poly6*(h^2-r^2)^3
 // term by term; here the cubes of each neighbour row are summed with fused
 // multiply-adds, the nine row sums are added with compensation (Kahan) and
-// the total is scaled once: the two differ by float rounding only (a row
-// holds a fifth of the terms; the row sums are what keeps a long sum of
-// clumped fluid accurate).
+// the total is scaled once: the two differ by float rounding only.  (A row's
+// sum costs one dependent operation per term instead of a four-operation
+// compensated step, which matters where clumped rows hold hundreds of terms;
+// the compensation across rows keeps the total's error at the level of one
+// row's.)
 //
 // A warp's particles are up to 32 consecutive cell-sorted particles of one
 // row of slots (my, mz), hence x-sorted, and share its nine neighbour rows.
