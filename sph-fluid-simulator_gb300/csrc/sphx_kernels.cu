@@ -1257,7 +1257,7 @@ __device__ __forceinline__ bool density_scan(const DensityChunk<kInd> &sm, uint3
         ++k;
     }
     const uint64_t PX = f32x2_dup(pi.x), PY = f32x2_dup(pi.y), PZ = f32x2_dup(pi.z);
-#pragma unroll 2
+#pragma unroll 4
     for (; k + 1u < hi; k += 2u) {
         const uint64_t X = *reinterpret_cast<const uint64_t *>(sm.x + k);
         if (f32x2_lo(X) > xhi) return true;
