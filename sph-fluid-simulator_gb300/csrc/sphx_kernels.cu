@@ -779,12 +779,10 @@ __device__ __forceinline__ void coop_rows_warp(const WalkCtx &W, const WalkStart
 }
 
 // What coop_walk does with the valid lanes off the cooperative path: walk
-// them alone with `vis` (kTailAll), walk them alone when they need no bucket
-// weights, i.e. sit at the grid's x seam (kTailRows: the caller has handed
-// the others to a later kernel), or leave them all to the caller
-// (kTailNone).  Keeping the slow walk, a call, out of a kernel frees its
-// register allocation.
-enum CoopTail { kTailNone, kTailRows, kTailAll };
+// them alone with `vis` (kTailAll) or leave them to the caller (kTailNone,
+// which lists them for a later kernel).  Keeping the slow walk, a call, out
+// of a kernel frees its register allocation.
+enum CoopTail { kTailNone, kTailAll };
 
 // Runs the scanner over every fast lane's neighbours, one group after
 // another (kWarpLoad: coop_rows_warp, else coop_rows_group), then the tail.
@@ -809,8 +807,6 @@ __device__ __forceinline__ void coop_walk(const WalkCtx &W, const WalkStart &s, 
         }
     }
     if (kTail == kTailAll && cl.valid && !cl.fast) walk<kInd>(W, s, self, pi, vis);
-    if (kTail == kTailRows && cl.valid && !cl.fast && s.flags == 0u)
-        walk_rows<kInd>(W, s.c, s.mx, s.my, s.mz, self, pi, vis);
 }
 
 // Appends the warp's lanes with `defer` set to a deferred list (*counter
